@@ -1,0 +1,149 @@
+/*
+ * C ABI of the GB300 multiplication hot path: exact products, squares and dense
+ * convolutions of 64-bit limb vectors on one GPU.
+ *
+ * Each entry point replaces one call of the reference crate `ntt_anafis` (paths are
+ * relative to that crate's root):
+ *
+ *   ntt_mul_plan_new            MulPlan::new                 src/plan.rs:53
+ *   ntt_mul_plan_mul_device     MulPlan::mul                 src/plan.rs:94
+ *   ntt_mul_plan_sqr_device     MulPlan::sqr                 src/plan.rs:112
+ *   ntt_mul_workspace_new/free  MulWorkspace::new            src/plan.rs:143
+ *   ntt_mul_workspace_prepare   MulWorkspace::prepare        src/plan.rs:151
+ *   ntt_mul_workspace_mul       MulWorkspace::mul            src/plan.rs:164
+ *   ntt_mul_workspace_sqr       MulWorkspace::sqr            src/plan.rs:177
+ *   ntt_conv_plan_new           ConvPlan::new                src/convolve.rs:75
+ *   ntt_conv_plan_convolve_device ConvPlan::convolve         src/convolve.rs:148
+ *   ntt_conv_workspace_new/free ConvWorkspace::new           src/convolve.rs:237
+ *   ntt_conv_workspace_prepare  ConvWorkspace::prepare       src/convolve.rs:246
+ *   ntt_conv_workspace_convolve ConvWorkspace::convolve      src/convolve.rs:264
+ *
+ * Conventions (as in the reference, src/lib.rs:1-24):
+ *  - limbs are uint64_t, least significant first;
+ *  - a product writes exactly a_len + b_len limbs, a square 2 * a_len limbs, a
+ *    convolution (a_len + b_len - 1) * stride limbs; limbs past that are preserved;
+ *  - every failure returns 0 and leaves dst unmodified; success returns 1;
+ *  - a == b with a_len == b_len (the same slice twice) runs the square path.
+ *
+ * Host-pointer calls (`*_mul`, `*_sqr`, `*_convolve`) copy the operands to the GPU,
+ * run, and copy the result back before returning. Pinned (page-locked) host buffers
+ * copy fastest. `*_device` calls take device pointers and a cudaStream_t (as
+ * void*), enqueue the work and return without synchronizing; the device buffers must
+ * stay valid until the stream reaches that point.
+ *
+ * A workspace owns device arenas that only grow and must not be used by two threads
+ * at once. Plans are plain values. The root tables are shared by all workspaces of a
+ * process and built once per device.
+ */
+#ifndef NTT_GB300_H
+#define NTT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Admitted product geometry (MulPlan). Fields are outputs of ntt_mul_plan_new. */
+typedef struct ntt_mul_plan {
+    uint64_t len_a;
+    uint64_t len_b;
+    uint32_t primes;          /* NTT primes used */
+    uint32_t log_transform;   /* log2 of the transform length */
+    uint64_t scratch_len;     /* device scratch limbs of ntt_mul_plan_mul_device */
+    uint64_t sqr_scratch_len; /* device scratch limbs of ntt_mul_plan_sqr_device */
+} ntt_mul_plan;
+
+/* Admitted convolution geometry (ConvPlan). */
+typedef struct ntt_conv_plan {
+    uint64_t len_a;
+    uint64_t len_b;
+    uint64_t max_a;
+    uint64_t max_b;
+    uint32_t is_signed;
+    uint32_t primes;          /* 0 when the short operand is summed directly */
+    uint32_t log_transform;
+    uint32_t schoolbook;      /* 1 when min(len_a, len_b) <= 24 */
+    uint64_t stride;          /* limbs per output coefficient */
+    uint64_t output_len;      /* (len_a + len_b - 1) * stride */
+    uint64_t scratch_len;     /* device scratch limbs of ntt_conv_plan_convolve_device */
+} ntt_conv_plan;
+
+typedef struct ntt_mul_workspace ntt_mul_workspace;
+typedef struct ntt_conv_workspace ntt_conv_workspace;
+
+/* Plans positive lengths; returns 0 (no plan) for a zero length or a shape beyond
+ * the GPU transform catalog (a_len + b_len - 1 > 2^25 coefficients). MulPlan::new,
+ * src/plan.rs:53. */
+int ntt_mul_plan_new(uint64_t len_a, uint64_t len_b, ntt_mul_plan* out);
+
+/* a*b into d_dst with caller-owned device scratch (MulPlan::mul, src/plan.rs:94). */
+uint8_t ntt_mul_plan_mul_device(const ntt_mul_plan* plan, uint64_t* d_dst, size_t dst_len,
+                                const uint64_t* d_a, size_t a_len, const uint64_t* d_b,
+                                size_t b_len, uint64_t* d_scratch, size_t scratch_len,
+                                void* stream);
+/* a*a (MulPlan::sqr, src/plan.rs:112). */
+uint8_t ntt_mul_plan_sqr_device(const ntt_mul_plan* plan, uint64_t* d_dst, size_t dst_len,
+                                const uint64_t* d_a, size_t a_len, uint64_t* d_scratch,
+                                size_t scratch_len, void* stream);
+
+/* Workspace bound to the current CUDA device (MulWorkspace::new, src/plan.rs:143);
+ * NULL when no device is available. */
+ntt_mul_workspace* ntt_mul_workspace_new(void);
+void ntt_mul_workspace_free(ntt_mul_workspace* ws);
+/* Retains the plan and grows the arenas (MulWorkspace::prepare, src/plan.rs:151).
+ * Returns 0 when device memory cannot be allocated. */
+uint8_t ntt_mul_workspace_prepare(ntt_mul_workspace* ws, const ntt_mul_plan* plan);
+/* MulWorkspace::mul (src/plan.rs:164): empty operands write zeros; a shape other
+ * than the retained plan is planned and retained. Host pointers. */
+uint8_t ntt_mul_workspace_mul(ntt_mul_workspace* ws, uint64_t* dst, size_t dst_len,
+                              const uint64_t* a, size_t a_len, const uint64_t* b, size_t b_len);
+/* MulWorkspace::sqr (src/plan.rs:177). Host pointers. */
+uint8_t ntt_mul_workspace_sqr(ntt_mul_workspace* ws, uint64_t* dst, size_t dst_len,
+                              const uint64_t* a, size_t a_len);
+/* Device-pointer forms of the two calls above, enqueued on `stream`. */
+uint8_t ntt_mul_workspace_mul_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_len,
+                                     const uint64_t* d_a, size_t a_len, const uint64_t* d_b,
+                                     size_t b_len, void* stream);
+uint8_t ntt_mul_workspace_sqr_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_len,
+                                     const uint64_t* d_a, size_t a_len, void* stream);
+
+/* ConvPlan::new (src/convolve.rs:75): bounds the magnitude of every coefficient;
+ * signed bounds must lie below 2^63. */
+int ntt_conv_plan_new(uint64_t len_a, uint64_t len_b, uint64_t max_a, uint64_t max_b,
+                      int is_signed, ntt_conv_plan* out);
+/* ConvPlan::convolve (src/convolve.rs:148) on device pointers with caller scratch.
+ * Coefficient bounds are checked on the host copy only in the host-pointer call;
+ * this call checks lengths and buffer sizes. */
+uint8_t ntt_conv_plan_convolve_device(const ntt_conv_plan* plan, uint64_t* d_dst,
+                                      size_t dst_len, const uint64_t* d_a, size_t a_len,
+                                      const uint64_t* d_b, size_t b_len, uint64_t* d_scratch,
+                                      size_t scratch_len, void* stream);
+
+ntt_conv_workspace* ntt_conv_workspace_new(void);
+void ntt_conv_workspace_free(ntt_conv_workspace* ws);
+/* ConvWorkspace::prepare (src/convolve.rs:246). */
+uint8_t ntt_conv_workspace_prepare(ntt_conv_workspace* ws, const ntt_conv_plan* plan);
+/* ConvWorkspace::convolve (src/convolve.rs:264): fails without a prepared plan, for
+ * mismatched lengths, a coefficient above its bound, or a short dst. Host pointers. */
+uint8_t ntt_conv_workspace_convolve(ntt_conv_workspace* ws, uint64_t* dst, size_t dst_len,
+                                    const uint64_t* a, size_t a_len, const uint64_t* b,
+                                    size_t b_len);
+/* Device-pointer form; coefficient bounds are the caller's responsibility. */
+uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_dst,
+                                           size_t dst_len, const uint64_t* d_a, size_t a_len,
+                                           const uint64_t* d_b, size_t b_len, void* stream);
+
+/* Message of the last failure on this thread ("" when none). */
+const char* ntt_last_error(void);
+/* Kernels launched by this process since load (counted per launch by the host). */
+uint64_t ntt_kernel_launches(void);
+/* Library version string. */
+const char* ntt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NTT_GB300_H */

@@ -1,0 +1,17 @@
+"""GB300-native exact big-integer multiplication: products, squares and dense
+convolutions of 64-bit limb vectors through multi-prime NTTs in hand-written
+sm_103a CUDA, behind the call shapes of ntt_anafis's MulPlan/MulWorkspace and
+ConvPlan/ConvWorkspace."""
+from .api import (  # noqa: F401
+    ConvPlan,
+    GpuConvWorkspace,
+    GpuMulWorkspace,
+    MulPlan,
+    exported_symbols,
+    kernel_launches,
+    last_error,
+    library,
+)
+from .operands import operand  # noqa: F401
+
+__version__ = "0.1.0"

@@ -1,0 +1,329 @@
+"""Python mirror of the reference's multiplication API over the GB300 C ABI.
+
+`MulPlan`, `GpuMulWorkspace`, `ConvPlan` and `GpuConvWorkspace` follow the call
+shapes of `ntt_anafis::{MulPlan, MulWorkspace, ConvPlan, ConvWorkspace}`
+(src/plan.rs:34-205, src/convolve.rs:52-281): operands and destinations are
+little-endian `uint64` limb vectors, calls return `True` on success and `False`
+on failure with the destination untouched, success preserves the destination's
+suffix, and passing the same array as both operands squares it.
+
+Host arrays are numpy `uint64` arrays (C-contiguous); device tensors are torch
+`int64`/`uint64` CUDA tensors, passed to the `*_device` methods together with a
+CUDA stream. There is no CPU fallback: without the compiled library every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libntt_gb300.so"
+_lib: Optional[ctypes.CDLL] = None
+
+u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class NttMulPlan(ctypes.Structure):
+    _fields_ = [
+        ("len_a", ctypes.c_uint64),
+        ("len_b", ctypes.c_uint64),
+        ("primes", ctypes.c_uint32),
+        ("log_transform", ctypes.c_uint32),
+        ("scratch_len", ctypes.c_uint64),
+        ("sqr_scratch_len", ctypes.c_uint64),
+    ]
+
+
+class NttConvPlan(ctypes.Structure):
+    _fields_ = [
+        ("len_a", ctypes.c_uint64),
+        ("len_b", ctypes.c_uint64),
+        ("max_a", ctypes.c_uint64),
+        ("max_b", ctypes.c_uint64),
+        ("is_signed", ctypes.c_uint32),
+        ("primes", ctypes.c_uint32),
+        ("log_transform", ctypes.c_uint32),
+        ("schoolbook", ctypes.c_uint32),
+        ("stride", ctypes.c_uint64),
+        ("output_len", ctypes.c_uint64),
+        ("scratch_len", ctypes.c_uint64),
+    ]
+
+
+# (name, restype, argtypes) of every exported entry point of include/ntt_gb300.h.
+_SIGNATURES = [
+    ("ntt_mul_plan_new", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(NttMulPlan)]),
+    ("ntt_mul_plan_mul_device", ctypes.c_uint8,
+     [ctypes.POINTER(NttMulPlan), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_mul_plan_sqr_device", ctypes.c_uint8,
+     [ctypes.POINTER(NttMulPlan), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_mul_workspace_new", ctypes.c_void_p, []),
+    ("ntt_mul_workspace_free", None, [ctypes.c_void_p]),
+    ("ntt_mul_workspace_prepare", ctypes.c_uint8, [ctypes.c_void_p, ctypes.POINTER(NttMulPlan)]),
+    ("ntt_mul_workspace_mul", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t]),
+    ("ntt_mul_workspace_sqr", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),
+    ("ntt_mul_workspace_mul_device", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_mul_workspace_sqr_device", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_conv_plan_new", ctypes.c_int,
+     [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+      ctypes.POINTER(NttConvPlan)]),
+    ("ntt_conv_plan_convolve_device", ctypes.c_uint8,
+     [ctypes.POINTER(NttConvPlan), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_conv_workspace_new", ctypes.c_void_p, []),
+    ("ntt_conv_workspace_free", None, [ctypes.c_void_p]),
+    ("ntt_conv_workspace_prepare", ctypes.c_uint8, [ctypes.c_void_p, ctypes.POINTER(NttConvPlan)]),
+    ("ntt_conv_workspace_convolve", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t]),
+    ("ntt_conv_workspace_convolve_device", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_last_error", ctypes.c_char_p, []),
+    ("ntt_kernel_launches", ctypes.c_uint64, []),
+    ("ntt_version", ctypes.c_char_p, []),
+]
+
+
+def library() -> ctypes.CDLL:
+    """Loads libntt_gb300.so (building it first if nvcc is present); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        from . import build_ext
+
+        try:
+            build_ext.build()
+        except Exception as exc:  # no toolkit: fail loudly, never fall back
+            raise RuntimeError(f"libntt_gb300.so is not built and cannot be built: {exc}") from exc
+    lib = ctypes.CDLL(str(_LIB_PATH))
+    for name, restype, argtypes in _SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return [name for name, _, _ in _SIGNATURES]
+
+
+def last_error() -> str:
+    return library().ntt_last_error().decode()
+
+
+def kernel_launches() -> int:
+    return int(library().ntt_kernel_launches())
+
+
+def _host(arr: np.ndarray, name: str) -> np.ndarray:
+    if not isinstance(arr, np.ndarray) or arr.dtype != np.uint64 or arr.ndim != 1:
+        raise TypeError(f"{name} must be a 1-D numpy uint64 array")
+    if not arr.flags["C_CONTIGUOUS"]:
+        raise TypeError(f"{name} must be contiguous")
+    return arr
+
+
+def _ptr(arr: np.ndarray) -> int:
+    return arr.ctypes.data if arr.size else 0
+
+
+def _dev(t) -> tuple[int, int]:
+    """(device pointer, element count) of a 1-D 64-bit CUDA tensor."""
+    if t.element_size() != 8 or t.dim() != 1 or not t.is_contiguous() or not t.is_cuda:
+        raise TypeError("device operands must be contiguous 1-D 64-bit CUDA tensors")
+    return int(t.data_ptr()), int(t.numel())
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        return 0
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+@dataclass(frozen=True)
+class MulPlan:
+    """An admitted product shape (ntt_anafis MulPlan, src/plan.rs:34-114)."""
+
+    len_a: int
+    len_b: int
+    primes: int
+    log_transform: int
+    scratch_len_limbs: int
+    sqr_scratch_len_limbs: int
+
+    @staticmethod
+    def new(len_a: int, len_b: int) -> Optional["MulPlan"]:
+        raw = NttMulPlan()
+        if not library().ntt_mul_plan_new(len_a, len_b, ctypes.byref(raw)):
+            return None
+        return MulPlan(raw.len_a, raw.len_b, raw.primes, raw.log_transform, raw.scratch_len,
+                       raw.sqr_scratch_len)
+
+    def scratch_len(self) -> int:
+        return self.scratch_len_limbs
+
+    def sqr_scratch_len(self) -> int:
+        return self.sqr_scratch_len_limbs
+
+    def _raw(self) -> NttMulPlan:
+        return NttMulPlan(self.len_a, self.len_b, self.primes, self.log_transform, self.scratch_len_limbs,
+                          self.sqr_scratch_len_limbs)
+
+    def mul_device(self, dst, a, b, scratch, stream=None) -> bool:
+        """a*b on device tensors with caller-owned device scratch (MulPlan::mul)."""
+        d, nd = _dev(dst)
+        pa, na = _dev(a)
+        pb, nb = _dev(b)
+        ps, ns = _dev(scratch)
+        return bool(library().ntt_mul_plan_mul_device(ctypes.byref(self._raw()), d, nd, pa, na, pb, nb, ps, ns,
+                                                      _stream_handle(stream)))
+
+    def sqr_device(self, dst, a, scratch, stream=None) -> bool:
+        d, nd = _dev(dst)
+        pa, na = _dev(a)
+        ps, ns = _dev(scratch)
+        return bool(library().ntt_mul_plan_sqr_device(ctypes.byref(self._raw()), d, nd, pa, na, ps, ns,
+                                                      _stream_handle(stream)))
+
+
+class GpuMulWorkspace:
+    """Retained device tables and arenas (ntt_anafis MulWorkspace, src/plan.rs:135-205)."""
+
+    def __init__(self) -> None:
+        self._lib = library()
+        self._ws = self._lib.ntt_mul_workspace_new()
+        if not self._ws:
+            raise RuntimeError(f"cannot create a GPU workspace: {last_error()}")
+
+    def close(self) -> None:
+        if getattr(self, "_ws", None):
+            self._lib.ntt_mul_workspace_free(self._ws)
+            self._ws = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def prepare(self, plan: MulPlan) -> bool:
+        return bool(self._lib.ntt_mul_workspace_prepare(self._ws, ctypes.byref(plan._raw())))
+
+    def mul(self, dst: np.ndarray, a: np.ndarray, b: np.ndarray) -> bool:
+        _host(dst, "dst"), _host(a, "a"), _host(b, "b")
+        return bool(self._lib.ntt_mul_workspace_mul(self._ws, _ptr(dst), dst.size, _ptr(a), a.size, _ptr(b),
+                                                    b.size))
+
+    def sqr(self, dst: np.ndarray, a: np.ndarray) -> bool:
+        _host(dst, "dst"), _host(a, "a")
+        return bool(self._lib.ntt_mul_workspace_sqr(self._ws, _ptr(dst), dst.size, _ptr(a), a.size))
+
+    def mul_device(self, dst, a, b, stream=None) -> bool:
+        d, nd = _dev(dst)
+        pa, na = _dev(a)
+        pb, nb = _dev(b)
+        return bool(self._lib.ntt_mul_workspace_mul_device(self._ws, d, nd, pa, na, pb, nb,
+                                                           _stream_handle(stream)))
+
+    def sqr_device(self, dst, a, stream=None) -> bool:
+        d, nd = _dev(dst)
+        pa, na = _dev(a)
+        return bool(self._lib.ntt_mul_workspace_sqr_device(self._ws, d, nd, pa, na, _stream_handle(stream)))
+
+
+@dataclass(frozen=True)
+class ConvPlan:
+    """An admitted convolution (ntt_anafis ConvPlan, src/convolve.rs:52-217)."""
+
+    len_a: int
+    len_b: int
+    max_a: int
+    max_b: int
+    signed: bool
+    primes: int
+    log_transform: int
+    schoolbook: bool
+    stride_limbs: int
+    output_limbs: int
+    scratch_limbs: int
+
+    @staticmethod
+    def new(len_a: int, len_b: int, max_a: int, max_b: int, signed: bool = False) -> Optional["ConvPlan"]:
+        raw = NttConvPlan()
+        if not library().ntt_conv_plan_new(len_a, len_b, max_a, max_b, int(signed), ctypes.byref(raw)):
+            return None
+        return ConvPlan(raw.len_a, raw.len_b, raw.max_a, raw.max_b, bool(raw.is_signed), raw.primes,
+                        raw.log_transform, bool(raw.schoolbook), raw.stride, raw.output_len, raw.scratch_len)
+
+    def stride(self) -> int:
+        return self.stride_limbs
+
+    def output_len(self) -> int:
+        return self.output_limbs
+
+    def scratch_len(self) -> int:
+        return self.scratch_limbs
+
+    def _raw(self) -> NttConvPlan:
+        return NttConvPlan(self.len_a, self.len_b, self.max_a, self.max_b, int(self.signed), self.primes,
+                           self.log_transform, int(self.schoolbook), self.stride_limbs, self.output_limbs,
+                           self.scratch_limbs)
+
+    def convolve_device(self, dst, a, b, scratch, stream=None) -> bool:
+        d, nd = _dev(dst)
+        pa, na = _dev(a)
+        pb, nb = _dev(b)
+        ps, ns = _dev(scratch) if scratch is not None else (0, 0)
+        return bool(library().ntt_conv_plan_convolve_device(ctypes.byref(self._raw()), d, nd, pa, na, pb, nb,
+                                                            ps, ns, _stream_handle(stream)))
+
+
+class GpuConvWorkspace:
+    """Retained convolution storage (ntt_anafis ConvWorkspace, src/convolve.rs:229-281)."""
+
+    def __init__(self) -> None:
+        self._lib = library()
+        self._ws = self._lib.ntt_conv_workspace_new()
+        if not self._ws:
+            raise RuntimeError(f"cannot create a GPU workspace: {last_error()}")
+
+    def close(self) -> None:
+        if getattr(self, "_ws", None):
+            self._lib.ntt_conv_workspace_free(self._ws)
+            self._ws = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def prepare(self, plan: ConvPlan) -> bool:
+        return bool(self._lib.ntt_conv_workspace_prepare(self._ws, ctypes.byref(plan._raw())))
+
+    def convolve(self, dst: np.ndarray, a: np.ndarray, b: np.ndarray) -> bool:
+        _host(dst, "dst"), _host(a, "a"), _host(b, "b")
+        return bool(self._lib.ntt_conv_workspace_convolve(self._ws, _ptr(dst), dst.size, _ptr(a), a.size,
+                                                          _ptr(b), b.size))
+
+    def convolve_device(self, dst, a, b, stream=None) -> bool:
+        d, nd = _dev(dst)
+        pa, na = _dev(a)
+        pb, nb = _dev(b)
+        return bool(self._lib.ntt_conv_workspace_convolve_device(self._ws, d, nd, pa, na, pb, nb,
+                                                                 _stream_handle(stream)))

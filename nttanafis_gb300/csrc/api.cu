@@ -1,0 +1,781 @@
+// Host side of the GB300 multiplication path: prime catalog, planner, device root
+// tables, workspaces and the C ABI declared in include/ntt_gb300.h.
+//
+// Planning mirrors the reference's admission rules (src/plan.rs:53-69,
+// src/convolve.rs:75-116, src/profile/planner.rs:120-322) with this library's own
+// geometry: every 64-bit limb is one transform coefficient, the transform length
+// is the power of two that holds the convolution, and the fewest 32-bit primes
+// whose product holds every coefficient are taken from a catalog of primes with
+// the needed two-power roots.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/ntt_gb300.h"
+#include "launch.h"
+
+namespace ntt {
+
+typedef unsigned __int128 u128;
+
+static thread_local std::string g_error;
+static std::atomic<uint64_t> g_launches{0};
+
+static bool fail(const char* msg) {
+    g_error = msg;
+    return false;
+}
+static bool cuda_ok(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return true;
+    g_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+// ---------------------------------------------------------------------------------
+// Prime catalog
+
+// Primes below 2^30 with 2-adic valuation of p-1 at least 21 (lazy arithmetic).
+static const u32 kLazyPrimes[] = {
+    1012924417u, 1004535809u, 998244353u, 985661441u, 975175681u, 962592769u, 950009857u,
+    943718401u,  935329793u,  924844033u, 918552577u, 899678209u, 897581057u, 880803841u,
+    824180737u,  799014913u,  786432001u, 754974721u, 740294657u, 715128833u, 710934529u,
+    683671553u,  666894337u,  648019969u, 645922817u, 639631361u, 635437057u, 597688321u,
+    595591169u,  576716801u,  469762049u, 463470593u, 459276289u, 415236097u, 387973121u,
+    383778817u,  377487361u,
+};
+// Primes below 2^31 with valuation at least 24 (canonical arithmetic, T >= 2^24).
+static const u32 kWidePrimes[] = {
+    2130706433u, 2113929217u, 2013265921u, 1811939329u, 1711276033u,
+    1224736769u, 1107296257u, 754974721u,  469762049u,  167772161u,
+};
+
+constexpr int kLazyMaxLog = 23;
+
+static u32 mulmod(u32 a, u32 b, u32 p) { return (u32)((u64)a * b % p); }
+static u32 powmod(u32 a, u64 e, u32 p) {
+    u32 r = 1 % p;
+    a %= p;
+    while (e) {
+        if (e & 1) r = mulmod(r, a, p);
+        a = mulmod(a, a, p);
+        e >>= 1;
+    }
+    return r;
+}
+static u32 invmod(u32 a, u32 p) { return powmod(a, p - 2, p); }
+static int valuation(u32 p) { return __builtin_ctz(p - 1); }
+
+static u32 generator(u32 p) {
+    u32 m = p - 1;
+    std::vector<u32> factors;
+    for (u32 q = 2; (u64)q * q <= m; ++q) {
+        if (m % q == 0) {
+            factors.push_back(q);
+            while (m % q == 0) m /= q;
+        }
+    }
+    if (m > 1) factors.push_back(m);
+    for (u32 g = 2; g < p; ++g) {
+        bool ok = true;
+        for (u32 q : factors)
+            if (powmod(g, (p - 1) / q, p) == 1) { ok = false; break; }
+        if (ok) return g;
+    }
+    return 0;
+}
+
+static std::vector<u32> primes_for(int log_t) {
+    std::vector<u32> out;
+    if (log_t <= kLazyMaxLog) {
+        for (u32 p : kLazyPrimes) if (valuation(p) >= log_t) out.push_back(p);
+    } else {
+        for (u32 p : kWidePrimes) if (valuation(p) >= log_t) out.push_back(p);
+    }
+    std::sort(out.begin(), out.end(), [](u32 x, u32 y) { return x > y; });
+    if (out.size() > (size_t)kMaxPrimes) out.resize(kMaxPrimes);
+    return out;
+}
+
+// Multiword helpers in radix 2^32, least significant first.
+typedef std::vector<u32> Words;
+static Words words_mul_small(const Words& a, u32 m) {
+    Words r(a.size() + 1, 0);
+    u64 c = 0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        const u64 t = (u64)a[i] * m + c;
+        r[i] = (u32)t;
+        c = t >> 32;
+    }
+    r[a.size()] = (u32)c;
+    while (r.size() > 1 && r.back() == 0) r.pop_back();
+    return r;
+}
+static int words_bitlen(const Words& a) {
+    for (int i = (int)a.size() - 1; i >= 0; --i)
+        if (a[i]) return i * 32 + 32 - __builtin_clz(a[i]);
+    return 0;
+}
+static u32 words_mod(const Words& a, u32 p) {
+    u64 r = 0;
+    for (int i = (int)a.size() - 1; i >= 0; --i) r = ((r << 32) | a[i]) % p;
+    return (u32)r;
+}
+
+// Coefficient capacity of the first np primes: X < 2^cap satisfies X <= P/2.
+static int capacity(const std::vector<u32>& primes, int np) {
+    Words P{1};
+    for (int i = 0; i < np; ++i) P = words_mul_small(P, primes[i]);
+    return words_bitlen(P) - 2;
+}
+
+static int ceil_log2(u64 x) { return x <= 1 ? 0 : 64 - __builtin_clzll(x - 1); }
+
+// ---------------------------------------------------------------------------------
+// Plans
+
+struct Geom {
+    bool conv = false;
+    u64 la = 0, lb = 0, conv_len = 0, out_len = 0;
+    int log_t = 0, np = 0, wide = 0, cap = 0;
+    u32 primes[kMaxPrimes] = {};
+    // convolutions
+    u64 max_a = 0, max_b = 0;
+    int sign = 0, bound_bits = 0, schoolbook = 0;
+    u64 stride = 1;
+
+    bool matches(u64 a, u64 b) const { return a == la && b == lb; }
+    u64 spec_words(bool square) const { return (u64)(square ? 1 : 2) * np * ((u64)1 << log_t); }
+    u64 scratch_bytes(bool square) const {
+        if (conv && schoolbook) return 0;
+        const u64 spec = (spec_words(square) * 4 + 255) & ~(u64)255;
+        return spec + (conv ? 0 : carry_scratch_bytes(out_len));
+    }
+};
+
+static bool choose_primes(Geom& g, int need_bits) {
+    const std::vector<u32> cand = primes_for(g.log_t);
+    for (int np = 1; np <= (int)cand.size(); ++np) {
+        const int cap = capacity(cand, np);
+        if (cap >= need_bits) {
+            g.np = np;
+            g.cap = cap;
+            for (int i = 0; i < np; ++i) g.primes[i] = cand[i];
+            g.wide = g.log_t > kLazyMaxLog;
+            return true;
+        }
+    }
+    return false;
+}
+
+static bool plan_mul(u64 la, u64 lb, Geom& g) {
+    if (!la || !lb) return fail("operand length is zero");
+    if (la > ((u64)1 << kMaxLogT) || lb > ((u64)1 << kMaxLogT) ||
+        la + lb - 1 > ((u64)1 << kMaxLogT))
+        return fail("product exceeds 2^25 transform coefficients");
+    g = Geom();
+    g.la = la;
+    g.lb = lb;
+    g.conv_len = la + lb - 1;
+    g.out_len = la + lb;
+    g.log_t = std::max(4, ceil_log2(g.conv_len));
+    const int need = 128 + ceil_log2(std::min(la, lb));
+    if (!choose_primes(g, need)) return fail("no prime set holds the coefficients");
+    return true;
+}
+
+static int bitlen128(u128 x) {
+    const u64 hi = (u64)(x >> 64), lo = (u64)x;
+    if (hi) return 128 - __builtin_clzll(hi);
+    if (lo) return 64 - __builtin_clzll(lo);
+    return 0;
+}
+
+// Bit length of terms*max_a*max_b (src/convolve.rs:358-369).
+static int bound_bits(u64 terms, u64 max_a, u64 max_b) {
+    const u128 product = (u128)max_a * max_b;
+    const u128 bound = product * terms;
+    const bool overflow = terms != 0 && bound / terms != product;
+    if (!overflow) return bitlen128(bound);
+    return bitlen128(product) + (terms > 1 ? 64 - __builtin_clzll(terms - 1) : 0);
+}
+
+static bool plan_conv(u64 la, u64 lb, u64 max_a, u64 max_b, int sign, Geom& g) {
+    if (!la || !lb) return fail("operand length is zero");
+    g = Geom();
+    g.conv = true;
+    g.la = la;
+    g.lb = lb;
+    g.max_a = max_a;
+    g.max_b = max_b;
+    g.sign = sign ? 1 : 0;
+    const u64 shorter = std::min(la, lb);
+    auto value_bits = [&](u64 m) { return (m ? 64 - __builtin_clzll(m) : 0) + g.sign; };
+    if (value_bits(max_a) > 64 || value_bits(max_b) > 64)
+        return fail("signed coefficient bound must lie below 2^63");
+    g.bound_bits = bound_bits(shorter, max_a, max_b) + g.sign;
+    g.stride = std::max<u64>(1, ((u64)g.bound_bits + 63) / 64);
+    if (la > ((u64)1 << 40) || lb > ((u64)1 << 40)) return fail("convolution length out of range");
+    g.conv_len = la + lb - 1;
+    g.out_len = g.conv_len * g.stride;
+    g.schoolbook = shorter <= 24;
+    if (!g.schoolbook) {
+        if (g.conv_len > ((u64)1 << kMaxLogT)) return fail("convolution exceeds 2^25 transform coefficients");
+        g.log_t = std::max(4, ceil_log2(g.conv_len));
+        if (!choose_primes(g, std::max(1, g.bound_bits))) return fail("no prime set holds the coefficients");
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------------
+// Device root tables (immutable once built; shared by all workspaces of a device)
+
+struct PrimeTables {
+    uint2* fwd = nullptr;
+    uint2* inv = nullptr;
+};
+struct StepTables {
+    uint2* f_lo = nullptr;
+    uint2* f_hi = nullptr;
+    uint2* i_lo = nullptr;
+    uint2* i_hi = nullptr;
+    uint2 scale{0, 0};
+};
+
+static std::mutex g_table_mutex;
+static std::map<std::pair<int, u32>, PrimeTables> g_prime_tables;
+static std::map<std::tuple<int, u32, int>, StepTables> g_step_tables;
+static std::map<int, bool> g_device_ready;
+
+static uint2 shoup_pair(u32 w, u32 p) { return make_uint2(w, (u32)(((u64)w << 32) / p)); }
+
+static bool upload(uint2** dst, const std::vector<uint2>& host) {
+    if (!cuda_ok(cudaMalloc((void**)dst, host.size() * sizeof(uint2)), "cudaMalloc(table)")) return false;
+    return cuda_ok(cudaMemcpy(*dst, host.data(), host.size() * sizeof(uint2), cudaMemcpyHostToDevice),
+                   "cudaMemcpy(table)");
+}
+
+static bool device_ready(int dev) {
+    if (g_device_ready[dev]) return true;
+    if (!cuda_ok(init_transform_kernels(), "kernel attributes")) return false;
+    if (!cuda_ok(init_crt_kernels(), "kernel attributes")) return false;
+    g_device_ready[dev] = true;
+    return true;
+}
+
+static bool prime_tables(int dev, u32 p, PrimeTables& out) {
+    auto key = std::make_pair(dev, p);
+    auto it = g_prime_tables.find(key);
+    if (it != g_prime_tables.end()) { out = it->second; return true; }
+    const u32 g = generator(p);
+    const int n = 1 << kMaxBlockLog;
+    std::vector<uint2> fwd(n), inv(n);
+    fwd[0] = inv[0] = shoup_pair(1, p);
+    for (int h = 1; h < n; h <<= 1) {
+        const u32 root = powmod(g, (p - 1) / (2 * (u64)h), p);
+        const u32 iroot = invmod(root, p);
+        u32 w = 1, iw = 1;
+        for (int j = 0; j < h; ++j) {
+            fwd[h + j] = shoup_pair(w, p);
+            inv[h + j] = shoup_pair(iw, p);
+            w = mulmod(w, root, p);
+            iw = mulmod(iw, iroot, p);
+        }
+    }
+    PrimeTables t;
+    if (!upload(&t.fwd, fwd) || !upload(&t.inv, inv)) return false;
+    g_prime_tables[key] = t;
+    out = t;
+    return true;
+}
+
+static int s_bits_of(int log_t) { return (log_t + 1) / 2; }
+
+static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
+    auto key = std::make_tuple(dev, p, log_t);
+    auto it = g_step_tables.find(key);
+    if (it != g_step_tables.end()) { out = it->second; return true; }
+    const u32 g = generator(p);
+    const u32 w = powmod(g, (p - 1) >> log_t, p);
+    const u32 iw = invmod(w, p);
+    // Inverse scale: T^-1 times 2^32 (undoes the Montgomery pointwise product).
+    const u32 scale = mulmod(invmod((u32)(((u64)1 << log_t) % p), p), (u32)(((u64)1 << 32) % p), p);
+    StepTables t;
+    t.scale = shoup_pair(scale, p);
+    if (log_t > kMaxBlockLog) {
+        const int s = s_bits_of(log_t);
+        const int nlo = 1 << s, nhi = 1 << (log_t - s);
+        std::vector<uint2> flo(nlo), ilo(nlo), fhi(nhi), ihi(nhi);
+        u32 x = 1, ix = 1;
+        for (int e = 0; e < nlo; ++e) {
+            flo[e] = shoup_pair(x, p);
+            ilo[e] = shoup_pair(ix, p);
+            x = mulmod(x, w, p);
+            ix = mulmod(ix, iw, p);
+        }
+        const u32 ws = powmod(w, (u64)1 << s, p), iws = powmod(iw, (u64)1 << s, p);
+        x = 1;
+        ix = scale;
+        for (int e = 0; e < nhi; ++e) {
+            fhi[e] = shoup_pair(x, p);
+            ihi[e] = shoup_pair(ix, p);
+            x = mulmod(x, ws, p);
+            ix = mulmod(ix, iws, p);
+        }
+        if (!upload(&t.f_lo, flo) || !upload(&t.f_hi, fhi) || !upload(&t.i_lo, ilo) || !upload(&t.i_hi, ihi))
+            return false;
+    }
+    g_step_tables[key] = t;
+    out = t;
+    return true;
+}
+
+// Fills the kernel constants of a plan; builds missing tables on the current device.
+static std::map<std::tuple<int, int, int>, std::pair<PrimeSet, CrtParams>> g_param_cache;
+
+static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
+    std::lock_guard<std::mutex> lock(g_table_mutex);
+    const auto key = std::make_tuple(dev, g.log_t, g.np);
+    auto hit = g_param_cache.find(key);
+    if (hit != g_param_cache.end()) {
+        ps = hit->second.first;
+        cp = hit->second.second;
+        cp.stride = (int)g.stride;
+        cp.bias = g.sign ? 0.5f : 0.25f;
+        return true;
+    }
+    if (!device_ready(dev)) return false;
+    memset(&ps, 0, sizeof(ps));
+    memset(&cp, 0, sizeof(cp));
+    Words P{1};
+    for (int i = 0; i < g.np; ++i) P = words_mul_small(P, g.primes[i]);
+    cp.np = g.np;
+    cp.l64 = std::min(4, (g.cap + 63) / 64);
+    cp.stride = (int)g.stride;
+    cp.bias = g.sign ? 0.5f : 0.25f;
+    for (int w = 0; w < (int)P.size() && w < kMaxPrimes; ++w) cp.P[w] = P[w];
+    for (int i = 0; i < g.np; ++i) {
+        const u32 p = g.primes[i];
+        PrimeTables pt;
+        StepTables st;
+        if (!prime_tables(dev, p, pt) || !step_tables(dev, p, g.log_t, st)) return false;
+        PrimeParams& pp = ps.pr[i];
+        pp.p = p;
+        u32 pinv = 1;  // p^-1 mod 2^32 by Newton's iteration (bits double each step)
+        for (int k = 0; k < 5; ++k) pinv *= 2u - p * pinv;
+        pp.pni = 0u - pinv;
+        pp.inv2_32 = (u32)(((u64)1 << 32) / p);
+        const u32 r32 = (u32)(((u64)1 << 32) % p);
+        pp.neg64 = mulmod(r32, r32, p);
+        pp.r32 = shoup_pair(r32, p);
+        pp.scale = st.scale;
+        pp.fwd = pt.fwd;
+        pp.inv = pt.inv;
+        pp.f4_lo = st.f_lo;
+        pp.f4_hi = st.f_hi;
+        pp.i4_lo = st.i_lo;
+        pp.i4_hi = st.i_hi;
+        // CRT cofactors M_i = P / p_i and their inverses.
+        Words M{1};
+        for (int j = 0; j < g.np; ++j) if (j != i) M = words_mul_small(M, g.primes[j]);
+        for (int w = 0; w < (int)M.size() && w < kMaxPrimes; ++w) cp.M[i][w] = M[w];
+        cp.p[i] = p;
+        cp.inv[i] = shoup_pair(invmod(words_mod(M, p), p), p);
+        cp.pinv[i] = 1.0f / (float)p;
+    }
+    g_param_cache[key] = std::make_pair(ps, cp);
+    return true;
+}
+
+// ---------------------------------------------------------------------------------
+// Execution on device pointers
+
+static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst,
+                    void* scratch, cudaStream_t st) {
+    if (g.conv && g.schoolbook) {
+        g_launches += 1;
+        return cuda_ok(launch_conv_schoolbook(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst,
+                                              (int)g.stride, g.sign != 0, st),
+                       "conv schoolbook launch");
+    }
+    TransformArgs ta;
+    memset(&ta, 0, sizeof(ta));
+    CrtParams cp;
+    if (!prepare_params(g, ta.ps, cp)) return false;
+    ta.a = d_a;
+    ta.b = square ? d_a : d_b;
+    ta.la = g.la;
+    ta.lb = square ? g.la : g.lb;
+    ta.spec = (u32*)scratch;
+    ta.conv_len = g.conv_len;
+    ta.np = g.np;
+    ta.log_t = g.log_t;
+    ta.wide = g.wide;
+    const bool sign = g.sign != 0;
+    if (g.log_t <= kMaxBlockLog) {
+        g_launches += 1;
+        if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
+    } else {
+        ta.log_r = g.log_t / 2;
+        ta.log_c = g.log_t - ta.log_r;
+        const int G = std::min(32, std::max(8, (1 << kMaxBlockLog) >> ta.log_r));
+        ta.log_g = __builtin_ctz(G);
+        int vs = ta.log_r >= 5 ? (1 << ta.log_r) + (1 << (ta.log_r - 5)) : (1 << ta.log_r);
+        const int target = 32 / G;
+        vs += ((target - vs) % 32 + 32) % 32;
+        ta.vstride_col = vs;
+        ta.s_bits = s_bits_of(g.log_t);
+        g_launches += 3;
+        if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) return false;
+        if (!cuda_ok(launch_rows(ta, square, st), "row pass launch")) return false;
+        if (!cuda_ok(launch_inv_cols(ta, st), "inverse column pass launch")) return false;
+    }
+    if (g.conv) {
+        g_launches += 1;
+        return cuda_ok(launch_crt_conv(ta.spec, g.log_t, g.conv_len, d_dst, sign, cp, st), "CRT launch");
+    }
+    const u64 spec_bytes = (g.spec_words(square) * 4 + 255) & ~(u64)255;
+    g_launches += 3;
+    return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst,
+                                  (uint8_t*)scratch + spec_bytes, cp, st),
+                   "CRT launch");
+}
+
+// Grow-only device buffer.
+struct DeviceBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    bool ensure(size_t need) {
+        if (need <= bytes) return true;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        if (!cuda_ok(cudaMalloc(&ptr, std::max<size_t>(need, 256)), "cudaMalloc(arena)")) return false;
+        bytes = std::max<size_t>(need, 256);
+        return true;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+static bool coefficients_admitted(const Geom& g, const u64* v, u64 n, u64 max) {
+    if (g.sign) {
+        for (u64 i = 0; i < n; ++i) {
+            const int64_t s = (int64_t)v[i];
+            const u64 mag = s < 0 ? (u64)0 - (u64)s : (u64)s;
+            if (mag > max) return false;
+        }
+        return true;
+    }
+    u64 acc = 0;
+    for (u64 i = 0; i < n; ++i) acc |= v[i];
+    if (acc <= max) return true;
+    for (u64 i = 0; i < n; ++i) if (v[i] > max) return false;
+    return true;
+}
+
+}  // namespace ntt
+
+using namespace ntt;
+
+// ---------------------------------------------------------------------------------
+// Workspaces
+
+struct ntt_mul_workspace {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool has_plan = false;
+    Geom plan;
+    DeviceBuf a, b, out, scratch;
+};
+
+struct ntt_conv_workspace {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool has_plan = false;
+    Geom plan;
+    DeviceBuf a, b, out, scratch;
+};
+
+template <class W>
+static W* workspace_new() {
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return nullptr;
+    W* ws = new W();
+    ws->device = dev;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
+        delete ws;
+        return nullptr;
+    }
+    return ws;
+}
+
+template <class W>
+static void workspace_free(W* ws) {
+    if (!ws) return;
+    cudaSetDevice(ws->device);
+    cudaStreamSynchronize(ws->stream);
+    ws->a.release();
+    ws->b.release();
+    ws->out.release();
+    ws->scratch.release();
+    cudaStreamDestroy(ws->stream);
+    delete ws;
+}
+
+// Runs a host-pointer call: copy in, execute, check, copy the result prefix out.
+template <class W>
+static bool run_host(W* ws, const Geom& g, bool square, u64* dst, const u64* a, const u64* b) {
+    const size_t out_bytes = g.out_len * sizeof(u64);
+    if (!ws->a.ensure(g.la * 8) || (!square && !ws->b.ensure(g.lb * 8)) || !ws->out.ensure(out_bytes) ||
+        !ws->scratch.ensure(g.scratch_bytes(square)))
+        return false;
+    cudaStream_t st = ws->stream;
+    if (!cuda_ok(cudaMemcpyAsync(ws->a.ptr, a, g.la * 8, cudaMemcpyHostToDevice, st), "copy a")) return false;
+    if (!square && !cuda_ok(cudaMemcpyAsync(ws->b.ptr, b, g.lb * 8, cudaMemcpyHostToDevice, st), "copy b"))
+        return false;
+    if (!execute(g, square, (const u64*)ws->a.ptr, (const u64*)ws->b.ptr, (u64*)ws->out.ptr, ws->scratch.ptr, st))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "kernels")) return false;
+    if (!cuda_ok(cudaMemcpyAsync(dst, ws->out.ptr, out_bytes, cudaMemcpyDeviceToHost, st), "copy dst")) return false;
+    return cuda_ok(cudaStreamSynchronize(st), "copy dst");
+}
+
+extern "C" {
+
+int ntt_mul_plan_new(uint64_t len_a, uint64_t len_b, ntt_mul_plan* out) {
+    Geom g;
+    if (!out || !plan_mul(len_a, len_b, g)) return 0;
+    out->len_a = len_a;
+    out->len_b = len_b;
+    out->primes = (uint32_t)g.np;
+    out->log_transform = (uint32_t)g.log_t;
+    out->scratch_len = (g.scratch_bytes(false) + 7) / 8;
+    out->sqr_scratch_len = (g.scratch_bytes(true) + 7) / 8;
+    return 1;
+}
+
+static uint8_t plan_run_device(const ntt_mul_plan* plan, bool square, uint64_t* d_dst, size_t dst_len,
+                               const uint64_t* d_a, size_t a_len, const uint64_t* d_b, size_t b_len,
+                               uint64_t* d_scratch, size_t scratch_len, void* stream) {
+    Geom g;
+    if (!plan || !plan_mul(plan->len_a, plan->len_b, g)) return 0;
+    if (!g.matches(a_len, b_len)) return fail("operand lengths differ from the plan");
+    if (square && a_len != b_len) return fail("a square needs a square plan");
+    if (dst_len < g.out_len) return fail("destination is shorter than the product");
+    if ((u64)scratch_len * 8 < g.scratch_bytes(square)) return fail("scratch is too short");
+    return execute(g, square, d_a, square ? d_a : d_b, d_dst, d_scratch, (cudaStream_t)stream);
+}
+
+uint8_t ntt_mul_plan_mul_device(const ntt_mul_plan* plan, uint64_t* d_dst, size_t dst_len, const uint64_t* d_a,
+                                size_t a_len, const uint64_t* d_b, size_t b_len, uint64_t* d_scratch,
+                                size_t scratch_len, void* stream) {
+    const bool alias = d_a == d_b && a_len == b_len;
+    return plan_run_device(plan, alias, d_dst, dst_len, d_a, a_len, d_b, b_len, d_scratch, scratch_len, stream);
+}
+
+uint8_t ntt_mul_plan_sqr_device(const ntt_mul_plan* plan, uint64_t* d_dst, size_t dst_len, const uint64_t* d_a,
+                                size_t a_len, uint64_t* d_scratch, size_t scratch_len, void* stream) {
+    return plan_run_device(plan, true, d_dst, dst_len, d_a, a_len, d_a, a_len, d_scratch, scratch_len, stream);
+}
+
+ntt_mul_workspace* ntt_mul_workspace_new(void) { return workspace_new<ntt_mul_workspace>(); }
+void ntt_mul_workspace_free(ntt_mul_workspace* ws) { workspace_free(ws); }
+
+static bool mul_reserve(ntt_mul_workspace* ws, const Geom& g, bool host) {
+    if (host && (!ws->a.ensure(g.la * 8) || !ws->b.ensure(g.lb * 8) || !ws->out.ensure(g.out_len * 8)))
+        return false;
+    if (!ws->scratch.ensure(g.scratch_bytes(false))) return false;
+    PrimeSet ps;
+    CrtParams cp;
+    return prepare_params(g, ps, cp);
+}
+
+uint8_t ntt_mul_workspace_prepare(ntt_mul_workspace* ws, const ntt_mul_plan* plan) {
+    if (!ws || !plan) return fail("null argument");
+    Geom g;
+    if (!plan_mul(plan->len_a, plan->len_b, g)) return 0;
+    cudaSetDevice(ws->device);
+    if (!mul_reserve(ws, g, true)) return 0;
+    ws->plan = g;
+    ws->has_plan = true;
+    return 1;
+}
+
+// Empty operands, plan retention and the destination check of MulWorkspace::run
+// (src/plan.rs:182-205).
+static int mul_admit(ntt_mul_workspace* ws, size_t dst_len, size_t a_len, size_t b_len, Geom& g) {
+    if (a_len == 0 || b_len == 0) {
+        if ((u64)a_len + b_len > dst_len) {
+            fail("destination is shorter than the product");
+            return -1;
+        }
+        return 0;  // zero product
+    }
+    if (ws->has_plan && ws->plan.matches(a_len, b_len)) {
+        g = ws->plan;
+    } else {
+        if (!plan_mul(a_len, b_len, g)) return -1;
+        ws->plan = g;
+        ws->has_plan = true;
+    }
+    if (dst_len < g.out_len) {
+        fail("destination is shorter than the product");
+        return -1;
+    }
+    return 1;
+}
+
+static uint8_t ws_mul_host(ntt_mul_workspace* ws, uint64_t* dst, size_t dst_len, const uint64_t* a, size_t a_len,
+                           const uint64_t* b, size_t b_len, bool square) {
+    if (!ws) return fail("null workspace");
+    Geom g;
+    const int adm = mul_admit(ws, dst_len, a_len, b_len, g);
+    if (adm < 0) return 0;
+    if (adm == 0) {
+        memset(dst, 0, ((size_t)a_len + b_len) * 8);
+        return 1;
+    }
+    if (!cuda_ok(cudaSetDevice(ws->device), "cudaSetDevice")) return 0;
+    return run_host(ws, g, square, dst, a, b) ? 1 : 0;
+}
+
+uint8_t ntt_mul_workspace_mul(ntt_mul_workspace* ws, uint64_t* dst, size_t dst_len, const uint64_t* a,
+                              size_t a_len, const uint64_t* b, size_t b_len) {
+    const bool alias = a == b && a_len == b_len;
+    return ws_mul_host(ws, dst, dst_len, a, a_len, b, b_len, alias);
+}
+
+uint8_t ntt_mul_workspace_sqr(ntt_mul_workspace* ws, uint64_t* dst, size_t dst_len, const uint64_t* a,
+                              size_t a_len) {
+    return ws_mul_host(ws, dst, dst_len, a, a_len, a, a_len, true);
+}
+
+static uint8_t ws_mul_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_len, const uint64_t* d_a,
+                             size_t a_len, const uint64_t* d_b, size_t b_len, bool square, void* stream) {
+    if (!ws) return fail("null workspace");
+    Geom g;
+    const int adm = mul_admit(ws, dst_len, a_len, b_len, g);
+    if (adm < 0) return 0;
+    if (!cuda_ok(cudaSetDevice(ws->device), "cudaSetDevice")) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (adm == 0)
+        return cuda_ok(cudaMemsetAsync(d_dst, 0, ((size_t)a_len + b_len) * 8, st), "zero product") ? 1 : 0;
+    if (!ws->scratch.ensure(g.scratch_bytes(square))) return 0;
+    return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, st) ? 1 : 0;
+}
+
+uint8_t ntt_mul_workspace_mul_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_len, const uint64_t* d_a,
+                                     size_t a_len, const uint64_t* d_b, size_t b_len, void* stream) {
+    const bool alias = d_a == d_b && a_len == b_len;
+    return ws_mul_device(ws, d_dst, dst_len, d_a, a_len, d_b, b_len, alias, stream);
+}
+
+uint8_t ntt_mul_workspace_sqr_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_len, const uint64_t* d_a,
+                                     size_t a_len, void* stream) {
+    return ws_mul_device(ws, d_dst, dst_len, d_a, a_len, d_a, a_len, true, stream);
+}
+
+// ---------------------------------------------------------------------------------
+// Convolutions
+
+int ntt_conv_plan_new(uint64_t len_a, uint64_t len_b, uint64_t max_a, uint64_t max_b, int is_signed,
+                      ntt_conv_plan* out) {
+    Geom g;
+    if (!out || !plan_conv(len_a, len_b, max_a, max_b, is_signed, g)) return 0;
+    out->len_a = len_a;
+    out->len_b = len_b;
+    out->max_a = max_a;
+    out->max_b = max_b;
+    out->is_signed = (uint32_t)g.sign;
+    out->primes = g.schoolbook ? 0 : (uint32_t)g.np;
+    out->log_transform = g.schoolbook ? 0 : (uint32_t)g.log_t;
+    out->schoolbook = (uint32_t)g.schoolbook;
+    out->stride = g.stride;
+    out->output_len = g.out_len;
+    out->scratch_len = (g.scratch_bytes(false) + 7) / 8;
+    return 1;
+}
+
+static bool conv_geom(const ntt_conv_plan* plan, Geom& g) {
+    return plan && plan_conv(plan->len_a, plan->len_b, plan->max_a, plan->max_b, (int)plan->is_signed, g);
+}
+
+uint8_t ntt_conv_plan_convolve_device(const ntt_conv_plan* plan, uint64_t* d_dst, size_t dst_len,
+                                      const uint64_t* d_a, size_t a_len, const uint64_t* d_b, size_t b_len,
+                                      uint64_t* d_scratch, size_t scratch_len, void* stream) {
+    Geom g;
+    if (!conv_geom(plan, g)) return 0;
+    if (!g.matches(a_len, b_len)) return fail("operand lengths differ from the plan");
+    if (dst_len < g.out_len) return fail("destination is shorter than the convolution");
+    const bool square = d_a == d_b && a_len == b_len;
+    if ((u64)scratch_len * 8 < g.scratch_bytes(square)) return fail("scratch is too short");
+    return execute(g, square, d_a, d_b, d_dst, d_scratch, (cudaStream_t)stream) ? 1 : 0;
+}
+
+ntt_conv_workspace* ntt_conv_workspace_new(void) { return workspace_new<ntt_conv_workspace>(); }
+void ntt_conv_workspace_free(ntt_conv_workspace* ws) { workspace_free(ws); }
+
+uint8_t ntt_conv_workspace_prepare(ntt_conv_workspace* ws, const ntt_conv_plan* plan) {
+    if (!ws) return fail("null workspace");
+    Geom g;
+    if (!conv_geom(plan, g)) return 0;
+    if (!cuda_ok(cudaSetDevice(ws->device), "cudaSetDevice")) return 0;
+    if (!ws->a.ensure(g.la * 8) || !ws->b.ensure(g.lb * 8) || !ws->out.ensure(g.out_len * 8) ||
+        !ws->scratch.ensure(g.scratch_bytes(false)))
+        return 0;
+    if (!g.schoolbook) {
+        PrimeSet ps;
+        CrtParams cp;
+        if (!prepare_params(g, ps, cp)) return 0;
+    }
+    ws->plan = g;
+    ws->has_plan = true;
+    return 1;
+}
+
+uint8_t ntt_conv_workspace_convolve(ntt_conv_workspace* ws, uint64_t* dst, size_t dst_len, const uint64_t* a,
+                                    size_t a_len, const uint64_t* b, size_t b_len) {
+    if (!ws) return fail("null workspace");
+    if (!ws->has_plan) return fail("no prepared plan");
+    const Geom& g = ws->plan;
+    if (!g.matches(a_len, b_len)) return fail("operand lengths differ from the plan");
+    if (!coefficients_admitted(g, a, a_len, g.max_a) || !coefficients_admitted(g, b, b_len, g.max_b))
+        return fail("a coefficient exceeds its bound");
+    if (dst_len < g.out_len) return fail("destination is shorter than the convolution");
+    if (!cuda_ok(cudaSetDevice(ws->device), "cudaSetDevice")) return 0;
+    const bool square = a == b && a_len == b_len;
+    return run_host(ws, g, square, dst, a, b) ? 1 : 0;
+}
+
+uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_dst, size_t dst_len,
+                                           const uint64_t* d_a, size_t a_len, const uint64_t* d_b, size_t b_len,
+                                           void* stream) {
+    if (!ws) return fail("null workspace");
+    if (!ws->has_plan) return fail("no prepared plan");
+    const Geom& g = ws->plan;
+    if (!g.matches(a_len, b_len)) return fail("operand lengths differ from the plan");
+    if (dst_len < g.out_len) return fail("destination is shorter than the convolution");
+    if (!cuda_ok(cudaSetDevice(ws->device), "cudaSetDevice")) return 0;
+    const bool square = d_a == d_b && a_len == b_len;
+    if (!ws->scratch.ensure(g.scratch_bytes(square))) return 0;
+    return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, (cudaStream_t)stream) ? 1 : 0;
+}
+
+const char* ntt_last_error(void) { return g_error.c_str(); }
+uint64_t ntt_kernel_launches(void) { return g_launches.load(); }
+const char* ntt_version(void) { return "nttanafis_gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

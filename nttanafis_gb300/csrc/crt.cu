@@ -1,0 +1,328 @@
+// Exact CRT reconstruction fused with the windowed limb sum and the carry scan,
+// the disjoint-block convolution output, and the short-operand column sums.
+//
+// Reference: cofactor CRT with one approximate quotient (src/limb/cofactor.rs:59-111),
+// coefficients added at bit i*w with carries across ranges
+// (src/limb/reconstruction.rs:77-483), signed offsets for convolutions
+// (src/limb/reconstruction.rs:94-163), and direct column sums for short operands
+// (src/convolve.rs:188-351).
+//
+// Here every product coefficient is a 64-bit-limb convolution value, so coefficient
+// k lands at limb k and spans l64 limbs. One CTA owns 1024 output limbs: it
+// reconstructs the coefficients that reach them, sums the overlapping windows,
+// propagates carries inside the tile with a generate/propagate block scan and
+// records the tile's (generate, propagate) pair. A one-CTA scan then resolves the
+// carry into every tile and a third kernel applies it (at most a run of all-ones
+// limbs). No kernel waits on another CTA.
+#include "launch.h"
+
+namespace ntt {
+
+constexpr int kCrtThreads = 256;
+
+// Reconstructs coefficient k from its residues: returns four u64 words of
+// S - q*P, S = sum_i y_i*(P/p_i), y_i = x_i*(P/p_i)^-1 mod p_i, q rounded from
+// sum_i y_i/p_i. Unsigned: 0 <= X < P/2. Signed: two's complement, |X| <= P/4.
+template <int NP>
+__device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log_t, u64 k,
+                                          const CrtParams& cp, u64 out[4]) {
+    u32 y[NP];
+    float f = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const u32 x = __ldg(resid + ((size_t)i << log_t) + k);
+        const u32 p = cp.p[i];
+        u32 v = shoup_mul(x, cp.inv[i].x, cp.inv[i].y, p);
+        v = sub_if_ge(v, p);
+        y[i] = v;
+        f = fmaf((float)v, cp.pinv[i], f);
+    }
+    constexpr int MW = NP > 1 ? NP - 1 : 1;  // words of P/p_i
+    u64 acc[NP + 1];
+#pragma unroll
+    for (int w = 0; w <= NP; ++w) acc[w] = 0;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+#pragma unroll
+        for (int w = 0; w < MW; ++w) {
+            const u64 pr = (u64)y[i] * cp.M[i][w];
+            acc[w] += (u32)pr;
+            acc[w + 1] += pr >> 32;
+        }
+    }
+    const u32 q = (u32)(f + cp.bias);
+    u32 x[NP + 1];
+    u64 carry = 0, mul = 0;
+    int64_t borrow = 0;
+#pragma unroll
+    for (int w = 0; w < NP; ++w) {
+        const u64 s = acc[w] + carry;
+        carry = s >> 32;
+        mul += (u64)q * cp.P[w];
+        const int64_t d = (int64_t)(u32)s - (int64_t)(u32)mul + borrow;
+        mul >>= 32;
+        x[w] = (u32)d;
+        borrow = d >> 32;  // 0 or -1
+    }
+    // Sign word: S fits NP words, so the result's top is the borrow alone.
+    x[NP] = (u32)borrow;
+    const u64 fill = borrow ? ~0ull : 0ull;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const int lo = 2 * w, hi = 2 * w + 1;
+        const u64 l = lo < NP ? (u64)x[lo] : (lo == NP ? (u64)x[NP] : fill & 0xffffffffull);
+        const u64 h = hi < NP ? (u64)x[hi] : (hi == NP ? (u64)x[NP] : fill & 0xffffffffull);
+        out[w] = l | (h << 32);
+    }
+}
+
+__device__ __forceinline__ void compose(u32& g, u32& p, u32 g_earlier, u32 p_earlier) {
+    g = g | (p & g_earlier);
+    p = p & p_earlier;
+}
+
+// Block-wide exclusive scan of carry (generate, propagate) pairs; returns the
+// exclusive pair in (g, p) and the inclusive total of the block in (tg, tp).
+__device__ __forceinline__ void block_scan_gp(u32& g, u32& p, u32& tg, u32& tp) {
+    __shared__ u32 wg[32], wp[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    u32 ig = g, ip = p;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const u32 og = __shfl_up_sync(0xffffffffu, ig, d);
+        const u32 op = __shfl_up_sync(0xffffffffu, ip, d);
+        if (lane >= d) compose(ig, ip, og, op);
+    }
+    if (lane == 31) { wg[warp] = ig; wp[warp] = ip; }
+    __syncthreads();
+    if (warp == 0) {
+        u32 a = lane < nwarps ? wg[lane] : 0u, b = lane < nwarps ? wp[lane] : 1u;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const u32 og = __shfl_up_sync(0xffffffffu, a, d);
+            const u32 op = __shfl_up_sync(0xffffffffu, b, d);
+            if (lane >= d) compose(a, b, og, op);
+        }
+        if (lane < nwarps) { wg[lane] = a; wp[lane] = b; }
+    }
+    __syncthreads();
+    // exclusive inside the warp
+    u32 eg = __shfl_up_sync(0xffffffffu, ig, 1), ep = __shfl_up_sync(0xffffffffu, ip, 1);
+    if (lane == 0) { eg = 0; ep = 1; }
+    if (warp > 0) compose(eg, ep, wg[warp - 1], wp[warp - 1]);
+    g = eg;
+    p = ep;
+    tg = wg[nwarps - 1];
+    tp = wp[nwarps - 1];
+}
+
+// Tile of kCrtTile output limbs; each thread owns four consecutive limbs.
+template <int NP>
+__global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__ resid, int log_t,
+                                                          u64 conv_len, u64 out_len, u64* __restrict__ dst,
+                                                          uint8_t* __restrict__ agg,
+                                                          const __grid_constant__ CrtParams cp) {
+    constexpr int kBack = 4;  // coefficients before the tile that reach into it (l64 <= 4)
+    __shared__ u64 xs[(kCrtTile + kBack) * 4];
+    const u64 j0 = (u64)blockIdx.x * kCrtTile;
+    for (int kk = threadIdx.x; kk < kCrtTile + kBack; kk += blockDim.x) {
+        const int64_t k = (int64_t)j0 - kBack + kk;
+        u64 w[4] = {0, 0, 0, 0};
+        if (k >= 0 && (u64)k < conv_len) crt_coeff<NP>(resid, log_t, (u64)k, cp, w);
+        xs[kk * 4 + 0] = w[0];
+        xs[kk * 4 + 1] = w[1];
+        xs[kk * 4 + 2] = w[2];
+        xs[kk * 4 + 3] = w[3];
+    }
+    __syncthreads();
+    const int L = cp.l64;
+    // Window sum of limb j0 + rel: low word and the count of overflows.
+    auto limb_sum = [&](int rel, u32& hi) -> u64 {
+        u64 lo = 0;
+        hi = 0;
+        for (int w = 0; w < L; ++w) {
+            const u64 v = xs[(rel - w + kBack) * 4 + w];
+            lo += v;
+            hi += (lo < v) ? 1u : 0u;
+        }
+        return lo;
+    };
+    const int base = threadIdx.x * 4;
+    u32 hprev;
+    limb_sum(base - 1, hprev);
+    u64 r[4];
+    u32 gm = 0, pm = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        u32 h;
+        const u64 lo = limb_sum(base + t, h);
+        const u64 s = lo + hprev;
+        gm |= (s < lo ? 1u : 0u) << t;
+        pm |= (s == ~0ull ? 1u : 0u) << t;
+        r[t] = s;
+        hprev = h;
+    }
+    // Thread composite over its four limbs, earliest first.
+    u32 G = 0, P = 1;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        u32 g = (gm >> t) & 1u, p = (pm >> t) & 1u;
+        compose(g, p, G, P);
+        G = g;
+        P = p;
+    }
+    u32 tg, tp;
+    block_scan_gp(G, P, tg, tp);
+    u32 c = G;  // carry into this thread's first limb when the tile's carry-in is zero
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const u64 j = j0 + base + t;
+        const u64 v = r[t] + c;
+        c = ((gm >> t) & 1u) | (((pm >> t) & 1u) & c);
+        if (j < out_len) dst[j] = v;
+    }
+    if (threadIdx.x == 0) agg[blockIdx.x] = (uint8_t)(tg | (tp << 1));
+}
+
+// Resolves the carry into every tile: cin[t] = carry out of tiles 0..t-1.
+__global__ void __launch_bounds__(1024) k_carry_scan(const uint8_t* __restrict__ agg, uint8_t* __restrict__ cin,
+                                                     int tiles) {
+    const int per = (tiles + blockDim.x - 1) / blockDim.x;
+    const int t0 = threadIdx.x * per;
+    u32 G = 0, P = 1;
+    for (int t = t0; t < t0 + per && t < tiles; ++t) {
+        u32 g = agg[t] & 1u, p = (agg[t] >> 1) & 1u;
+        compose(g, p, G, P);
+        G = g;
+        P = p;
+    }
+    u32 tg, tp;
+    block_scan_gp(G, P, tg, tp);
+    u32 c = G;
+    for (int t = t0; t < t0 + per && t < tiles; ++t) {
+        cin[t] = (uint8_t)c;
+        c = (agg[t] & 1u) | (((agg[t] >> 1) & 1u) & c);
+    }
+}
+
+// Adds a carry of one into each tile that receives it.
+__global__ void __launch_bounds__(kCrtThreads) k_carry_apply(u64* __restrict__ dst, u64 out_len,
+                                                              const uint8_t* __restrict__ cin) {
+    if (!cin[blockIdx.x]) return;
+    __shared__ unsigned long long first;
+    const u64 j0 = (u64)blockIdx.x * kCrtTile;
+    const u64 end = min(j0 + (u64)kCrtTile, out_len);
+    if (threadIdx.x == 0) first = end;
+    __syncthreads();
+    unsigned long long mine = end;
+    for (u64 j = j0 + threadIdx.x; j < end; j += blockDim.x)
+        if (dst[j] != ~0ull) { mine = j; break; }
+    atomicMin(&first, mine);
+    __syncthreads();
+    const u64 f = first;
+    for (u64 j = j0 + threadIdx.x; j < end; j += blockDim.x) {
+        if (j < f) dst[j] = 0;
+        else if (j == f) dst[j] += 1;
+    }
+}
+
+// Disjoint blocks: coefficient k fills limbs [k*stride, (k+1)*stride).
+template <int NP>
+__global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict__ resid, int log_t,
+                                                           u64 conv_len, u64* __restrict__ dst,
+                                                           const __grid_constant__ CrtParams cp) {
+    const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= conv_len) return;
+    u64 w[4];
+    crt_coeff<NP>(resid, log_t, k, cp, w);
+    const u64 fill = (w[3] >> 63) ? ~0ull : 0ull;
+    u64* out = dst + k * (u64)cp.stride;
+    for (int s = 0; s < cp.stride; ++s) out[s] = s < 4 ? w[s] : fill;
+}
+
+// Short operand (<= 24 terms): exact sums of 128-bit products in three limbs.
+template <bool SIGNED>
+__global__ void __launch_bounds__(kCrtThreads) k_conv_school(const u64* __restrict__ a, u64 la,
+                                                              const u64* __restrict__ b, u64 lb,
+                                                              u64* __restrict__ dst, int stride) {
+    const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k + 1 >= la + lb) return;
+    const u64 i_lo = k + 1 > lb ? k + 1 - lb : 0;
+    const u64 i_hi = min(k, la - 1);
+    u64 w0 = 0, w1 = 0, w2 = 0;
+    for (u64 i = i_lo; i <= i_hi; ++i) {
+        const u64 x = a[i], y = b[k - i];
+        const u64 lo = x * y;
+        const u64 hi = SIGNED ? (u64)__mul64hi((long long)x, (long long)y) : __umul64hi(x, y);
+        w0 += lo;
+        const u64 c0 = w0 < lo ? 1 : 0;
+        const u64 t = w1 + hi;
+        const u64 c1 = t < hi ? 1 : 0;
+        w1 = t + c0;
+        const u64 c2 = w1 < c0 ? 1 : 0;
+        w2 += c1 + c2;
+        if (SIGNED && (int64_t)hi < 0) w2 -= 1;
+    }
+    u64* out = dst + k * (u64)stride;
+    const u64 fill = (SIGNED && (int64_t)w2 < 0) ? ~0ull : 0ull;
+    for (int s = 0; s < stride; ++s) out[s] = s == 0 ? w0 : (s == 1 ? w1 : (s == 2 ? w2 : fill));
+}
+
+// ---------------------------------------------------------------------------------
+
+template <int NP>
+static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
+                       const CrtParams& cp, cudaStream_t st) {
+    const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
+    k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst, agg, cp);
+    k_carry_scan<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles);
+    k_carry_apply<<<tiles, kCrtThreads, 0, st>>>(dst, out_len, agg + tiles);
+}
+
+cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
+                           const CrtParams& cp, cudaStream_t st) {
+    switch (cp.np) {
+        case 1: crt_mul_np<1>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 2: crt_mul_np<2>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 3: crt_mul_np<3>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 4: crt_mul_np<4>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 5: crt_mul_np<5>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 6: crt_mul_np<6>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 7: crt_mul_np<7>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 8: crt_mul_np<8>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst, bool sign,
+                            const CrtParams& cp, cudaStream_t st) {
+    (void)sign;  // the quotient bias in cp selects signed rounding
+    const unsigned blocks = (unsigned)((conv_len + kCrtThreads - 1) / kCrtThreads);
+    switch (cp.np) {
+        case 1: k_crt_conv<1><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 2: k_crt_conv<2><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 3: k_crt_conv<3><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 4: k_crt_conv<4><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 5: k_crt_conv<5><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 6: k_crt_conv<6><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 7: k_crt_conv<7><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 8: k_crt_conv<8><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst, int stride,
+                                   bool sign, cudaStream_t st) {
+    const u64 n = la + lb - 1;
+    const unsigned blocks = (unsigned)((n + kCrtThreads - 1) / kCrtThreads);
+    if (sign) k_conv_school<true><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride);
+    else k_conv_school<false><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride);
+    return cudaGetLastError();
+}
+
+cudaError_t init_crt_kernels() { return cudaSuccess; }
+
+}  // namespace ntt

@@ -1,0 +1,70 @@
+// Host-side launch interface between the planner/workspaces and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ntt_arith.cuh"
+
+namespace ntt {
+
+// Largest transform held by one CTA, and the longest in-CTA vector of the
+// four-step passes (C = 2^13 u32 rows, R = 2^12 u32 columns).
+constexpr int kMaxBlockLog = 13;
+// Largest transform length handled at all (coefficients of a product or convolution).
+constexpr int kMaxLogT = 25;
+// Output limbs per CTA of the CRT + carry kernel.
+constexpr int kCrtTile = 1024;
+
+// Operands and geometry of one transform-domain product.
+struct TransformArgs {
+    const u64* a;
+    const u64* b;
+    u64 la, lb;
+    u32* spec;         // [2][np][T] residues; region 0 ends as the product residues
+    u64 conv_len;      // coefficients of the product/convolution
+    int np;            // primes
+    int log_t;         // log2 transform length
+    int log_r, log_c;  // four-step split T = R * C (unused on the one-CTA path)
+    int log_g;         // log2 columns per CTA in the column passes
+    int vstride_col;   // padded words per column vector in shared memory
+    int s_bits;        // low-digit bits of the two-level four-step twiddle tables
+    int wide;          // 1: primes up to 2^31 in canonical arithmetic; 0: lazy, p < 2^30
+    PrimeSet ps;
+};
+
+// Exact-CRT constants of one prime set (words in radix 2^32).
+struct CrtParams {
+    int np;
+    int l64;                           // u64 words of one reconstructed coefficient
+    int stride;                        // output limbs per coefficient (convolutions)
+    float bias;                        // 0.25 unsigned, 0.5 signed quotient rounding
+    u32 p[kMaxPrimes];
+    uint2 inv[kMaxPrimes];             // (P/p_i)^-1 mod p_i with Shoup companion
+    float pinv[kMaxPrimes];            // 1/p_i in fp32
+    u32 M[kMaxPrimes][kMaxPrimes];     // P/p_i
+    u32 P[kMaxPrimes];                 // P
+};
+
+// Launchers; each returns the launch status.
+cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
+cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
+cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st);
+cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st);
+
+cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst,
+                           uint8_t* agg, const CrtParams& cp, cudaStream_t st);
+cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst, bool sign,
+                            const CrtParams& cp, cudaStream_t st);
+cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
+                                   int stride, bool sign, cudaStream_t st);
+// Scratch bytes the CRT carry pass needs for `out_len` output limbs.
+inline u64 carry_scratch_bytes(u64 out_len) {
+    const u64 tiles = (out_len + kCrtTile - 1) / kCrtTile;
+    return 2 * tiles + 16;
+}
+
+// One-time kernel attribute setup (shared-memory opt-in) for the current device.
+cudaError_t init_transform_kernels();
+cudaError_t init_crt_kernels();
+
+}  // namespace ntt
