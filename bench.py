@@ -1,0 +1,372 @@
+"""Throughput of exact 1,048,576 x 1,048,576-limb products on GB300.
+
+One step = one exact product of two 1M-limb operands (SplitMix64 seeds 1 and 2
+plus per-set offsets), the workload the reference's headline number is quoted on
+(README.md:28 of the reference: 43.4 ms on one Zen 5 core). Products are
+independent, so N GPUs run N replicas ("scaling": "weak") with no collective on
+the data path; the timed region is bracketed by a barrier and a device sync on
+every rank and the slowest rank's time counts.
+
+Printed keys beyond the base contract:
+  e2e         the same metric through the host-pointer C ABI call
+              (ntt_mul_workspace_mul) from pinned host buffers, copies included;
+  roofline    algorithmic bytes of one product (operands in, product out, and the
+              fused four-step spectrum traffic 8*S with S from the reference
+              planner) over the measured device time per product;
+  kernels     per-kernel device times from CUDA events recorded between the
+              library's launches on the launching stream;
+  cpu_baseline  the oracle (a C restatement of the reference algorithm) timed
+              on this host's cores on a bounded sample of the same workload.
+
+`--impl reference` times that CPU restatement alone (the reference crate is Rust
+and cannot be built here), with every host thread, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+LA = LB = 1 << 20
+L2_BYTES = 129 * 2**20
+WORKLOAD = "mul 1048576x1048576 u64 limbs (SplitMix64)"
+METRIC = "products/s (1,048,576 x 1,048,576-limb exact products)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def shard_units(units: int, rank: int, world: int) -> range:
+    """Replica sharding: rank r runs units r, r+world, ... (no data exchange)."""
+    return range(rank, units, world)
+
+
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peak_gbs() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        try:
+            return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{gpu_index}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxes.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = sorted(sms)[len(sms) // 2:] or sms
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": max(maxes), "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def operand_sets(count: int):
+    from nttanafis_gb300.operands import operand
+
+    return [(operand(LA, 1 + 2 * i), operand(LB, 2 + 2 * i)) for i in range(count)]
+
+
+def cpu_sample(threads: int, seconds: float = 12.0, max_products: int = 20) -> dict:
+    """Times the oracle on whole products until `seconds` elapse (bounded sample)."""
+    import oracle
+
+    from nttanafis_gb300.operands import operand
+
+    a, b = operand(LA, 1), operand(LB, 2)
+    oracle.mul(a, b, threads)  # tables, page-in
+    done, t0 = 0, time.perf_counter()
+    while done < max_products and (time.perf_counter() - t0 < seconds or done == 0):
+        oracle.mul(a, b, threads)
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "seconds_per_product": dt / done, "products": done, "threads": threads}
+
+
+def cpu_model() -> str:
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.machine()
+
+
+def run_reference(args) -> None:
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle
+
+    from nttanafis_gb300.operands import operand
+
+    threads = os.cpu_count() or 1
+    a, b = operand(LA, 1), operand(LB, 2)
+    for _ in range(args.warmup):
+        oracle.mul(a, b, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.mul(a, b, threads)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (SplitMix64 seeds 1, 2)",
+        "config": {"workload": WORKLOAD, "la": LA, "lb": LB, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "products/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} whole 1M x 1M products, {threads} threads, {cpu_model()}"},
+        "e2e": {"value": value, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    import oracle
+    import nttanafis_gb300 as ntt
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    lib = ntt.library()
+
+    per_step_in = 8 * (LA + LB)
+    nsets = max(2, -(-2 * L2_BYTES // per_step_in))  # rotating inputs larger than L2
+    host_sets = operand_sets(nsets)
+    d_a = [torch.from_numpy(a.view(np.int64)).to(dev) for a, _ in host_sets]
+    d_b = [torch.from_numpy(b.view(np.int64)).to(dev) for _, b in host_sets]
+    d_out = [torch.empty(LA + LB, dtype=torch.int64, device=dev) for _ in range(nsets)]
+    ws = ntt.GpuMulWorkspace()
+    plan = ntt.MulPlan.new(LA, LB)
+    assert ws.prepare(plan), ntt.last_error()
+    stream = torch.cuda.Stream(device=dev)
+
+    def step(i: int) -> None:
+        k = i % nsets
+        if not ws.mul_device(d_out[k], d_a[k], d_b[k], stream):
+            raise RuntimeError(ntt.last_error())
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step(i)
+    torch.cuda.synchronize(dev)
+
+    # Parity of the timed configuration against exact fingerprints.
+    from nttanafis_gb300.operands import to_int
+
+    A, B = to_int(host_sets[0][0]), to_int(host_sets[0][1])
+    C = to_int(d_out[0].cpu().numpy().view(np.uint64)) if args.warmup else None
+    fingerprint_ok = None
+    if C is not None:
+        qs = [(1 << 61) - 1, (1 << 89) - 1, (1 << 107) - 1]
+        fingerprint_ok = all((A % q) * (B % q) % q == C % q for q in qs)
+
+    sampler = ClockSampler(local)
+    launches0 = ntt.kernel_launches()
+    with sampler:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t_wall = time.perf_counter()
+        e0.record(stream)
+        for i in range(args.steps):
+            step(i)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_wall = time.perf_counter() - t_wall
+        if world > 1:
+            torch.distributed.barrier()
+        dev_ms = e0.elapsed_time(e1)
+        launches = ntt.kernel_launches() - launches0
+
+        # End to end through the host-pointer C ABI call, pinned host memory.
+        h_a = torch.from_numpy(host_sets[0][0].view(np.int64)).pin_memory()
+        h_b = torch.from_numpy(host_sets[0][1].view(np.int64)).pin_memory()
+        h_dst = torch.empty(LA + LB, dtype=torch.int64).pin_memory()
+        na, nb, nd = (x.numpy().view(np.uint64) for x in (h_a, h_b, h_dst))
+        e2e_steps = max(3, min(args.steps, 50))
+        for _ in range(2):
+            assert ws.mul(nd, na, nb), ntt.last_error()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ws.mul(nd, na, nb)
+        e2e_s = time.perf_counter() - t0
+        e2e_ok = fingerprint_ok is None or to_int(nd) % ((1 << 61) - 1) == (A % ((1 << 61) - 1)) * (
+            B % ((1 << 61) - 1)) % ((1 << 61) - 1)
+
+    max_ms = max_over_ranks(dev_ms, world, dev)
+    ms_per_step = max_ms / args.steps
+    value = world * args.steps / (max_ms / 1000.0)
+    e2e_value = world * e2e_steps / max_over_ranks(e2e_s, world, dev)
+
+    # Per-kernel device times: events recorded between the library's launches.
+    kernel_names = ["pack+column DIF (k_fwd_cols)", "row DIF+pointwise+DIT (k_rows)",
+                    "column DIT (k_inv_cols)", "CRT+window+tile carry (k_crt_mul)",
+                    "tile carry scan (k_carry_scan)", "carry apply (k_carry_apply)"]
+    import ctypes
+
+    reps = 10
+    stride = len(kernel_names) + 1
+    per_kernel = [0.0] * len(kernel_names)
+    ms = (ctypes.c_float * (reps * stride))()
+    lib.ntt_timing_start(reps * stride)
+    for r in range(reps):
+        step(r)
+    got = lib.ntt_timing_stop(ms, reps * stride)
+    timed_ok = got == reps * stride - 1
+    if timed_ok:
+        for r in range(reps):
+            for k in range(len(kernel_names)):
+                per_kernel[k] += ms[r * stride + k] / reps
+    kernels = [{"kernel": n_, "ms": round(t, 5)} for n_, t in zip(kernel_names, per_kernel)]
+    instrumented_ms = sum(per_kernel)
+    dominant = max(range(len(per_kernel)), key=lambda k: per_kernel[k]) if timed_ok else None
+
+    peak, peak_kind = measured_peak_gbs()
+    model = oracle.model_bytes("mul", LA, LB)
+    achieved = model / (ms_per_step / 1000.0) / 1e9
+    traffic = None
+    tpath = ROOT / "profiles" / "traffic_mul_1M.json"
+    if tpath.exists():
+        try:
+            traffic = json.loads(tpath.read_text()).get("dram_bytes_per_product")
+        except Exception:
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 modular (NTT primes < 2^31), u64 limbs", "data": "synthetic (SplitMix64)",
+        "config": {"workload": WORKLOAD, "la": LA, "lb": LB, "primes": plan.primes,
+                   "log_transform": plan.log_transform, "parallelism": f"replicas x{world}",
+                   "l2": f"inputs larger than L2: {nsets} rotating operand pairs ({nsets * per_step_in >> 20} MiB)"},
+        "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": per_step_in,
+                "d2h_bytes_per_step": 8 * (LA + LB), "api": "ntt_mul_workspace_mul (host pointers, pinned)",
+                "steps": e2e_steps, "parity_ok": bool(e2e_ok)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                     "traffic": traffic, "algorithmic_bytes": model,
+                     "unit_of_launch": "one product (the fused kernel sequence below)",
+                     "dominant_kernel": kernel_names[dominant] if dominant is not None else None},
+        "kernels": kernels, "kernels_ms_total": instrumented_ms,
+        "gpu_launches": launches, "wall_s": t_wall, "parity": {"fingerprint_ok": fingerprint_ok},
+    }
+    line["clocks"] = sampler.summary()
+    if rank == 0 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        multi = cpu_sample(cores, seconds=args.cpu_seconds)
+        single = cpu_sample(1, seconds=args.cpu_seconds / 2, max_products=3)
+        line["cpu_baseline"] = {
+            "value": multi["value"], "unit": "products/s", "cores": cores, "kind": "port",
+            "sample": (f"{multi['products']} whole 1M x 1M products on {cores} threads ({cpu_model()}); "
+                       f"single thread: {single['value']:.3f} products/s over {single['products']}"),
+            "single_thread_value": single["value"],
+        }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

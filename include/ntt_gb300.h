@@ -135,6 +135,15 @@ uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_d
                                            size_t dst_len, const uint64_t* d_a, size_t a_len,
                                            const uint64_t* d_b, size_t b_len, void* stream);
 
+/* Per-kernel timing for measurement tools (not thread-safe). After
+ * ntt_timing_start(count), each call records a CUDA event on its launching stream
+ * before its first kernel and after every kernel, until `count` events are used.
+ * ntt_timing_stop waits for the last event, writes the milliseconds between
+ * consecutive events into ms[0..capacity) and returns how many it wrote (-1 on a
+ * CUDA error), and switches timing off. */
+int ntt_timing_start(int count);
+int ntt_timing_stop(float* ms, int capacity);
+
 /* Message of the last failure on this thread ("" when none). */
 const char* ntt_last_error(void);
 /* Kernels launched by this process since load (counted per launch by the host). */

@@ -29,6 +29,17 @@ typedef unsigned __int128 u128;
 static thread_local std::string g_error;
 static std::atomic<uint64_t> g_launches{0};
 
+// Optional per-kernel timing: when set, an event is recorded on the launching
+// stream before the first kernel of a call and after every kernel.
+static std::vector<cudaEvent_t> g_events;
+static bool g_timing = false;
+static int g_marks_n = 0;
+static int g_marks_i = 0;
+
+void mark(cudaStream_t st) {
+    if (g_timing && g_marks_i < g_marks_n && cudaEventRecord(g_events[g_marks_i], st) == cudaSuccess) ++g_marks_i;
+}
+
 static bool fail(const char* msg) {
     g_error = msg;
     return false;
@@ -401,11 +412,14 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
 
 static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst,
                     void* scratch, cudaStream_t st) {
+    mark(st);
     if (g.conv && g.schoolbook) {
         g_launches += 1;
-        return cuda_ok(launch_conv_schoolbook(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst,
-                                              (int)g.stride, g.sign != 0, st),
-                       "conv schoolbook launch");
+        const bool ok = cuda_ok(launch_conv_schoolbook(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst,
+                                                       (int)g.stride, g.sign != 0, st),
+                                "conv schoolbook launch");
+        mark(st);
+        return ok;
     }
     TransformArgs ta;
     memset(&ta, 0, sizeof(ta));
@@ -424,6 +438,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
     if (g.log_t <= kMaxBlockLog) {
         g_launches += 1;
         if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
+        mark(st);
     } else {
         ta.log_r = g.log_t / 2;
         ta.log_c = g.log_t - ta.log_r;
@@ -436,17 +451,22 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         ta.s_bits = s_bits_of(g.log_t);
         g_launches += 3;
         if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) return false;
+        mark(st);
         if (!cuda_ok(launch_rows(ta, square, st), "row pass launch")) return false;
+        mark(st);
         if (!cuda_ok(launch_inv_cols(ta, st), "inverse column pass launch")) return false;
+        mark(st);
     }
     if (g.conv) {
         g_launches += 1;
-        return cuda_ok(launch_crt_conv(ta.spec, g.log_t, g.conv_len, d_dst, sign, cp, st), "CRT launch");
+        const bool ok = cuda_ok(launch_crt_conv(ta.spec, g.log_t, g.conv_len, d_dst, sign, cp, st), "CRT launch");
+        mark(st);
+        return ok;
     }
     const u64 spec_bytes = (g.spec_words(square) * 4 + 255) & ~(u64)255;
     g_launches += 3;
     return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst,
-                                  (uint8_t*)scratch + spec_bytes, cp, st),
+                                  (uint8_t*)scratch + spec_bytes, cp, st, mark),
                    "CRT launch");
 }
 
@@ -772,6 +792,34 @@ uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_d
     const bool square = d_a == d_b && a_len == b_len;
     if (!ws->scratch.ensure(g.scratch_bytes(square))) return 0;
     return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, (cudaStream_t)stream) ? 1 : 0;
+}
+
+int ntt_timing_start(int count) {
+    if (count < 2) return 0;
+    while ((int)g_events.size() < count) {
+        cudaEvent_t e;
+        if (!cuda_ok(cudaEventCreate(&e), "cudaEventCreate")) return 0;
+        g_events.push_back(e);
+    }
+    g_marks_n = count;
+    g_marks_i = 0;
+    g_timing = true;
+    return 1;
+}
+
+int ntt_timing_stop(float* ms, int capacity) {
+    const int n = g_marks_i;
+    g_timing = false;
+    g_marks_i = 0;
+    if (n < 2) return 0;
+    if (!cuda_ok(cudaEventSynchronize(g_events[n - 1]), "cudaEventSynchronize")) return -1;
+    int out = 0;
+    for (int i = 0; i + 1 < n && out < capacity; ++i) {
+        float t = 0.0f;
+        if (!cuda_ok(cudaEventElapsedTime(&t, g_events[i], g_events[i + 1]), "cudaEventElapsedTime")) return -1;
+        ms[out++] = t;
+    }
+    return out;
 }
 
 const char* ntt_last_error(void) { return g_error.c_str(); }

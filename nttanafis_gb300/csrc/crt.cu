@@ -273,24 +273,27 @@ __global__ void __launch_bounds__(kCrtThreads) k_conv_school(const u64* __restri
 
 template <int NP>
 static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
-                       const CrtParams& cp, cudaStream_t st) {
+                       const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
     const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
     k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst, agg, cp);
+    if (mark) mark(st);
     k_carry_scan<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles);
+    if (mark) mark(st);
     k_carry_apply<<<tiles, kCrtThreads, 0, st>>>(dst, out_len, agg + tiles);
+    if (mark) mark(st);
 }
 
 cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
-                           const CrtParams& cp, cudaStream_t st) {
+                           const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
     switch (cp.np) {
-        case 1: crt_mul_np<1>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 2: crt_mul_np<2>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 3: crt_mul_np<3>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 4: crt_mul_np<4>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 5: crt_mul_np<5>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 6: crt_mul_np<6>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 7: crt_mul_np<7>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
-        case 8: crt_mul_np<8>(resid, log_t, conv_len, out_len, dst, agg, cp, st); break;
+        case 1: crt_mul_np<1>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 2: crt_mul_np<2>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 3: crt_mul_np<3>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 4: crt_mul_np<4>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 5: crt_mul_np<5>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 6: crt_mul_np<6>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 7: crt_mul_np<7>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
+        case 8: crt_mul_np<8>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -52,7 +52,8 @@ cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st);
 cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st);
 
 cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst,
-                           uint8_t* agg, const CrtParams& cp, cudaStream_t st);
+                           uint8_t* agg, const CrtParams& cp, cudaStream_t st,
+                           void (*mark)(cudaStream_t) = nullptr);
 cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst, bool sign,
                             const CrtParams& cp, cudaStream_t st);
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,

@@ -1,0 +1,83 @@
+"""The C ABI library loads without a GPU, exports every declared symbol, and its
+planner follows the reference's admission rules."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import nttanafis_gb300 as ntt
+
+ROOT = Path(__file__).resolve().parents[1]
+MASK = (1 << 64) - 1
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "ntt_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ntt_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ntt.library()
+    names = declared_symbols()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+    assert sorted(ntt.exported_symbols()) == names
+
+
+def test_version_and_counters():
+    assert b"sm_103a" in ntt.library().ntt_version()
+    assert ntt.kernel_launches() >= 0
+
+
+def test_mul_plans_reject_like_the_reference(golden):
+    for la, lb in golden["rejections"]["mul_none"]:
+        assert ntt.MulPlan.new(la, lb) is None
+    for la, lb in [(1, 1), (3, 7), (4, 4), (16, 65), (257, 256)]:
+        p = ntt.MulPlan.new(la, lb)
+        assert p is not None and p.scratch_len() >= p.sqr_scratch_len()
+    assert ntt.MulPlan.new(2**25, 2) is None  # beyond the GPU transform catalog
+
+
+def test_conv_strides_match_reference_table(golden):
+    for terms, ma, mb, stride in golden["strides"]["cases"]:
+        assert ntt.ConvPlan.new(terms, terms, ma, mb, False).stride() == stride
+
+
+def test_conv_plans_reject_like_the_reference(golden):
+    for la, lb, ma, mb, s in golden["rejections"]["conv_none"]:
+        assert ntt.ConvPlan.new(la, lb, ma, mb, bool(s)) is None
+    p = ntt.ConvPlan.new(3, 2, 3, 5, False)
+    assert p.output_len() == 4 and p.scratch_len() == 0 and p.schoolbook
+    big = ntt.ConvPlan.new(30, 30, 7, 7, False)
+    assert big.scratch_len() > 0 and not big.schoolbook
+
+
+def test_conv_plan_matches_oracle_stride_and_output():
+    import oracle
+
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        la, lb = int(rng.integers(1, 5000)), int(rng.integers(1, 5000))
+        bits_a, bits_b = int(rng.integers(0, 65)), int(rng.integers(0, 65))
+        signed = bool(rng.integers(0, 2))
+        ma = (1 << bits_a) - 1 if bits_a < 64 else MASK
+        mb = (1 << bits_b) - 1 if bits_b < 64 else MASK
+        if signed:
+            ma, mb = min(ma, (1 << 63) - 1), min(mb, (1 << 63) - 1)
+        ours = ntt.ConvPlan.new(la, lb, ma, mb, signed)
+        ref = oracle.conv_plan(la, lb, ma, mb, signed)
+        assert (ours is None) == (ref is None)
+        if ours is not None:
+            assert ours.stride() == ref["stride"] and ours.output_len() == ref["output_len"]
+            assert ours.schoolbook == bool(ref["schoolbook"])
+
+
+def test_plans_hold_every_coefficient():
+    # capacity of the chosen primes covers 128 + ceil(log2(min)) bits
+    for la, lb in [(1, 1), (1024, 1024), (2**20, 2**20), (2**20, 131072), (2**24, 2**24), (2**25 - 5, 5)]:
+        p = ntt.MulPlan.new(la, lb)
+        assert p is not None, (la, lb)
+        assert (1 << p.log_transform) >= la + lb - 1

@@ -1,0 +1,189 @@
+"""Bit-exact parity of the CUDA path (through the C ABI) with the oracle, the
+golden Python-integer products, and modular fingerprints at full sizes."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from nttanafis_gb300.operands import operand, sparse_operand, to_int
+
+pytestmark = pytest.mark.gpu
+MASK = (1 << 64) - 1
+FINGERPRINT_PRIMES = [(1 << 61) - 1, (1 << 89) - 1, (1 << 107) - 1, (1 << 127) - 1]
+THREADS = os.cpu_count() or 1
+
+
+def hexlimbs(values):
+    return np.array([int(v, 16) for v in values], dtype=np.uint64)
+
+
+def all_ones_expected(la: int, lb: int) -> np.ndarray:
+    """Limbs of (B^la - 1)(B^lb - 1), src/tests/scheduling.rs:35-45."""
+    left, right = max(la, lb), min(la, lb)
+    out = np.zeros(la + lb, dtype=np.uint64)
+    out[0] = 1
+    out[right:] = MASK
+    out[left] = MASK - 1
+    return out
+
+
+def fingerprint_ok(a, b, c) -> bool:
+    A, B, C = to_int(a), to_int(b), to_int(c)
+    return all((A % q) * (B % q) % q == C % q for q in FINGERPRINT_PRIMES)
+
+
+@pytest.fixture(scope="module")
+def ws(gpu):
+    w = gpu.GpuMulWorkspace()
+    yield w
+    w.close()
+
+
+def gpu_mul(ws, a, b, extra=2):
+    dst = np.full(a.size + b.size + extra, MASK, dtype=np.uint64)
+    assert ws.mul(dst, a, b), "mul failed"
+    assert np.all(dst[a.size + b.size:] == MASK), "suffix was overwritten"
+    return dst[:a.size + b.size]
+
+
+def gpu_sqr(ws, a):
+    dst = np.full(2 * a.size + 1, MASK, dtype=np.uint64)
+    assert ws.sqr(dst, a), "sqr failed"
+    assert dst[-1] == MASK
+    return dst[:2 * a.size]
+
+
+def test_golden_products(ws, golden):
+    for case in golden["products"]["cases"]:
+        a, b = operand(case["la"], case["seed_a"]), operand(case["lb"], case["seed_b"])
+        got = gpu_mul(ws, a, b)
+        assert hashlib.sha256(got.astype("<u8").tobytes()).hexdigest() == case["sha256"], (case["la"], case["lb"])
+        if "product" in case:
+            assert np.array_equal(got, hexlimbs(case["product"]))
+
+
+def test_golden_squares(ws, golden):
+    for case in golden["squares"]["cases"]:
+        a = operand(case["la"], case["seed"])
+        assert np.array_equal(gpu_sqr(ws, a), hexlimbs(case["square"]))
+
+
+def test_config_1024_mul_and_sqr_match_oracle(ws):
+    a, b = operand(1024, 1), operand(1024, 2)
+    assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b))
+    assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a))
+
+
+def test_small_shapes_every_length(ws):
+    # proptest range of src/tests/products.rs:134-135: 1..=40 limbs each
+    rng = np.random.default_rng(11)
+    for la in range(1, 41):
+        for lb in (1, 2, 7, 16, 33, 40):
+            a = rng.integers(0, 2**64, la, dtype=np.uint64)
+            b = rng.integers(0, 2**64, lb, dtype=np.uint64)
+            assert np.array_equal(gpu_mul(ws, a, b), oracle.schoolbook(a, b)), (la, lb)
+        assert np.array_equal(gpu_sqr(ws, a), oracle.schoolbook(a, a)), la
+
+
+def test_unbalanced_either_order(ws):
+    # src/tests/products.rs:180-201: 1..=40 short, 200..=1500 long, both orders
+    rng = np.random.default_rng(12)
+    for _ in range(24):
+        short = rng.integers(0, 2**64, int(rng.integers(1, 41)), dtype=np.uint64)
+        long = rng.integers(0, 2**64, int(rng.integers(200, 1501)), dtype=np.uint64)
+        assert np.array_equal(gpu_mul(ws, long, short), oracle.mul(long, short))
+        assert np.array_equal(gpu_mul(ws, short, long), oracle.mul(short, long))
+
+
+@pytest.mark.parametrize("la,lb", [(4096, 4096), (4097, 4096), (8192, 8191), (8193, 8192), (20000, 13000),
+                                   (65536, 65536), (65536, 256), (131072, 131072), (300000, 250000),
+                                   (1 << 20, 131072)])
+def test_transform_classes_match_oracle(ws, la, lb):
+    # crosses the one-CTA / four-step boundary (T = 2^13 / 2^14) and every split
+    a, b = operand(la, 21), operand(lb, 22)
+    assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b, THREADS)), (la, lb)
+
+
+def test_config_1m_mul_and_sqr_match_oracle(ws):
+    a, b = operand(1 << 20, 1), operand(1 << 20, 2)
+    expected = oracle.mul(a, b, THREADS)
+    assert np.array_equal(gpu_mul(ws, a, b), expected)
+    assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a, THREADS))
+
+
+def test_edge_operands_all_ones_and_sparse(ws):
+    ones = np.full(1 << 20, MASK, dtype=np.uint64)
+    assert np.array_equal(gpu_mul(ws, ones, ones), all_ones_expected(1 << 20, 1 << 20))
+    a, b = sparse_operand(1 << 20, 3, 4), sparse_operand(1 << 20, 5, 6)
+    assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b, THREADS))
+    assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a, THREADS))
+    z = np.zeros(5000, dtype=np.uint64)
+    assert not np.any(gpu_mul(ws, z, operand(3000, 1)))
+
+
+@pytest.mark.parametrize("la,lb", [(4096, 64), (4097, 64), (5000, 300), (8192, 25), (3000, 1), (1 << 17, 1 << 17)])
+def test_all_ones_carries(ws, la, lb):
+    # src/tests/products.rs:17-29 and the closed form of src/tests/scheduling.rs:35-45
+    a = np.full(la, MASK, dtype=np.uint64)
+    b = np.full(lb, MASK, dtype=np.uint64)
+    assert np.array_equal(gpu_mul(ws, a, b), all_ones_expected(la, lb))
+    assert np.array_equal(gpu_mul(ws, b, a), all_ones_expected(la, lb))
+
+
+def test_wide_prime_class_2_pow_24(ws):
+    # T = 2^24 runs on the primes below 2^31 (canonical arithmetic)
+    a, b = operand(1 << 23, 31), operand((1 << 23) - 7, 32)
+    assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
+
+
+def test_config_16m_mul_and_sqr_fingerprints(ws):
+    a, b = operand(1 << 24, 1), operand(1 << 24, 2)
+    c = gpu_mul(ws, a, b, extra=1)
+    assert fingerprint_ok(a, b, c)
+    s = gpu_sqr(ws, a)
+    assert fingerprint_ok(a, a, s)
+
+
+def test_16m_all_ones(ws):
+    n = 1 << 24
+    ones = np.full(n, MASK, dtype=np.uint64)
+    assert np.array_equal(gpu_mul(ws, ones, ones, extra=0), all_ones_expected(n, n))
+
+
+def test_device_and_plan_scratch_paths(gpu):
+    import torch
+
+    la, lb = 70000, 50000
+    a, b = operand(la, 41), operand(lb, 42)
+    expected = oracle.mul(a, b, THREADS)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    db = torch.from_numpy(b.view(np.int64)).cuda()
+    dst = torch.full((la + lb + 3,), -1, dtype=torch.int64, device="cuda")
+    plan = gpu.MulPlan.new(la, lb)
+    scratch = torch.empty(plan.scratch_len(), dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    assert plan.mul_device(dst, da, db, scratch, stream)
+    torch.cuda.synchronize()
+    host = dst.cpu().numpy().view(np.uint64)
+    assert np.array_equal(host[:la + lb], expected) and np.all(host[la + lb:] == MASK)
+    # square through the plan with its smaller scratch
+    sq_plan = gpu.MulPlan.new(la, la)
+    sq_scratch = torch.empty(sq_plan.sqr_scratch_len(), dtype=torch.int64, device="cuda")
+    sq = torch.empty(2 * la, dtype=torch.int64, device="cuda")
+    assert sq_plan.sqr_device(sq, da, sq_scratch, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(sq.cpu().numpy().view(np.uint64), oracle.sqr(a, THREADS))
+    # workspace device path, aliasing the same tensor squares it
+    w = gpu.GpuMulWorkspace()
+    sq.fill_(0)
+    assert w.mul_device(sq, da, da, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(sq.cpu().numpy().view(np.uint64), oracle.sqr(a, THREADS))
+    # short scratch is rejected before any write
+    dst.fill_(-1)
+    assert not plan.mul_device(dst, da, db, scratch[:-1], stream)
+    torch.cuda.synchronize()
+    assert bool((dst == -1).all())
+    w.close()
