@@ -135,6 +135,28 @@ uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_d
                                            size_t dst_len, const uint64_t* d_a, size_t a_len,
                                            const uint64_t* d_b, size_t b_len, void* stream);
 
+/* Largest product (a_len + b_len - 1 coefficients) of ntt_mul_noalloc_device, and
+ * the device memory its static arrays hold on every GPU that loads the library. */
+#define NTT_NOALLOC_MAX_COEFFICIENTS 4096
+#define NTT_NOALLOC_SCRATCH_BYTES 164096
+#define NTT_NOALLOC_TABLE_BYTES 327680
+
+/* Exact product a*b (a*a when d_a == d_b and a_len == b_len) on device pointers for
+ * callers that must not allocate device memory: code running under a device-memory
+ * budget owned by another allocator, or on a latency-critical path where the
+ * device-wide synchronisation of cudaMalloc/cudaFree would stall other streams.
+ * It calls no allocating routine: its scratch and root tables are static device
+ * arrays that every GPU loading the library holds until exit. Limits:
+ * a_len + b_len - 1 <= NTT_NOALLOC_MAX_COEFFICIENTS (larger shapes return 0 with a
+ * message in ntt_last_error(), dst untouched); the first call on a device performs
+ * a one-time set-up with that device current, so make it before any stream capture;
+ * all calls share one scratch array, so calls that overlap on the GPU race - keep
+ * them ordered on one stream. Empty operands write zeros. Enqueues on `stream` and
+ * returns without synchronizing. This entry point has no counterpart in the
+ * reference crate. */
+uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const uint64_t* d_a, size_t a_len,
+                               const uint64_t* d_b, size_t b_len, void* stream);
+
 /* Per-kernel timing for measurement tools (not thread-safe). After
  * ntt_timing_start(count), each call records a CUDA event on its launching stream
  * before its first kernel and after every kernel, until `count` events are used.

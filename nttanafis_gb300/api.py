@@ -91,6 +91,9 @@ _SIGNATURES = [
     ("ntt_conv_workspace_convolve_device", ctypes.c_uint8,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_mul_noalloc_device", ctypes.c_uint8,
+     [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
     ("ntt_timing_start", ctypes.c_int, [ctypes.c_int]),
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_last_error", ctypes.c_char_p, []),

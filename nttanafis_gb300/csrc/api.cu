@@ -40,6 +40,8 @@ void mark(cudaStream_t st) {
     if (g_timing && g_marks_i < g_marks_n && cudaEventRecord(g_events[g_marks_i], st) == cudaSuccess) ++g_marks_i;
 }
 
+void set_last_error(const std::string& message) { g_error = message; }
+
 static bool fail(const char* msg) {
     g_error = msg;
     return false;

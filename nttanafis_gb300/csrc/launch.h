@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "ntt_arith.cuh"
 
 namespace ntt {
@@ -63,6 +65,9 @@ inline u64 carry_scratch_bytes(u64 out_len) {
     const u64 tiles = (out_len + kCrtTile - 1) / kCrtTile;
     return 2 * tiles + 16;
 }
+
+// Sets the message returned by ntt_last_error() on this thread.
+void set_last_error(const std::string& message);
 
 // One-time kernel attribute setup (shared-memory opt-in) for the current device.
 cudaError_t init_transform_kernels();
