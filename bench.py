@@ -285,7 +285,7 @@ def run_gpu(args) -> None:
     # Per-kernel device times: events recorded between the library's launches.
     kernel_names = ["pack+column DIF (k_fwd_cols)", "row DIF+pointwise+DIT (k_rows)",
                     "column DIT (k_inv_cols)", "CRT+window+tile carry (k_crt_mul)",
-                    "tile carry scan (k_carry_scan)", "carry apply (k_carry_apply)"]
+                    "tile carry scan and apply (k_carry)"]
     import ctypes
 
     reps = 10

@@ -466,7 +466,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         return ok;
     }
     const u64 spec_bytes = (g.spec_words(square) * 4 + 255) & ~(u64)255;
-    g_launches += 3;
+    g_launches += 2;
     return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst,
                                   (uint8_t*)scratch + spec_bytes, cp, st, mark),
                    "CRT launch");

@@ -117,77 +117,109 @@ __device__ __forceinline__ void block_scan_gp(u32& g, u32& p, u32& tg, u32& tp) 
     tp = wp[nwarps - 1];
 }
 
-// Tile of kCrtTile output limbs; each thread owns four consecutive limbs.
+// Inclusive warp scan of (generate, propagate) pairs over the lanes.
+__device__ __forceinline__ void warp_scan_gp(u32& g, u32& p) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const u32 og = __shfl_up_sync(0xffffffffu, g, d);
+        const u32 op = __shfl_up_sync(0xffffffffu, p, d);
+        if (lane >= d) compose(g, p, og, op);
+    }
+}
+
+// Tile of kCrtTile output limbs. Coefficient words sit in shared memory as four
+// word planes, so a warp reads consecutive 64-bit words. Warp w owns limbs
+// [128w, 128w + 128) of the tile; lane l handles limbs 32c + l of them (c < 4),
+// so every shared and global access of a warp is to consecutive words.
 template <int NP>
 __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__ resid, int log_t,
                                                           u64 conv_len, u64 out_len, u64* __restrict__ dst,
                                                           uint8_t* __restrict__ agg,
                                                           const __grid_constant__ CrtParams cp) {
     constexpr int kBack = 4;  // coefficients before the tile that reach into it (l64 <= 4)
-    __shared__ u64 xs[(kCrtTile + kBack) * 4];
+    constexpr int kWords = kCrtTile + kBack;
+    constexpr int kChunks = kCrtTile / (32 * (kCrtThreads / 32));  // 4 chunks of 32 limbs per warp
+    __shared__ u64 xs[4][kWords];
+    __shared__ u32 wsum_g[32], wsum_p[32];
     const u64 j0 = (u64)blockIdx.x * kCrtTile;
-    for (int kk = threadIdx.x; kk < kCrtTile + kBack; kk += blockDim.x) {
+    for (int kk = threadIdx.x; kk < kWords; kk += kCrtThreads) {
         const int64_t k = (int64_t)j0 - kBack + kk;
         u64 w[4] = {0, 0, 0, 0};
         if (k >= 0 && (u64)k < conv_len) crt_coeff<NP>(resid, log_t, (u64)k, cp, w);
-        xs[kk * 4 + 0] = w[0];
-        xs[kk * 4 + 1] = w[1];
-        xs[kk * 4 + 2] = w[2];
-        xs[kk * 4 + 3] = w[3];
+        xs[0][kk] = w[0];
+        xs[1][kk] = w[1];
+        xs[2][kk] = w[2];
+        xs[3][kk] = w[3];
     }
     __syncthreads();
     const int L = cp.l64;
-    // Window sum of limb j0 + rel: low word and the count of overflows.
+    // Window sum of limb j0 + rel: low word and the count of its overflows.
     auto limb_sum = [&](int rel, u32& hi) -> u64 {
         u64 lo = 0;
         hi = 0;
         for (int w = 0; w < L; ++w) {
-            const u64 v = xs[(rel - w + kBack) * 4 + w];
+            const u64 v = xs[w][rel - w + kBack];
             lo += v;
             hi += (lo < v) ? 1u : 0u;
         }
         return lo;
     };
-    const int base = threadIdx.x * 4;
-    u32 hprev;
-    limb_sum(base - 1, hprev);
-    u64 r[4];
-    u32 gm = 0, pm = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u64 r[kChunks];
+    u32 eg[kChunks], ep[kChunks], cg[kChunks], cpp[kChunks];
+    u32 WG = 0, WP = 1;  // composite of this warp's chunks so far
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        u32 h;
-        const u64 lo = limb_sum(base + t, h);
+    for (int c = 0; c < kChunks; ++c) {
+        const int rel = warp * 32 * kChunks + c * 32 + lane;
+        u32 hprev, h;
+        limb_sum(rel - 1, hprev);
+        const u64 lo = limb_sum(rel, h);
         const u64 s = lo + hprev;
-        gm |= (s < lo ? 1u : 0u) << t;
-        pm |= (s == ~0ull ? 1u : 0u) << t;
-        r[t] = s;
-        hprev = h;
+        r[c] = s;
+        u32 g = s < lo ? 1u : 0u, p = s == ~0ull ? 1u : 0u;
+        warp_scan_gp(g, p);
+        cg[c] = __shfl_sync(0xffffffffu, g, 31);
+        cpp[c] = __shfl_sync(0xffffffffu, p, 31);
+        u32 xg = __shfl_up_sync(0xffffffffu, g, 1), xp = __shfl_up_sync(0xffffffffu, p, 1);
+        if (lane == 0) { xg = 0; xp = 1; }
+        eg[c] = xg;
+        ep[c] = xp;
+        u32 ng = cg[c], np = cpp[c];
+        compose(ng, np, WG, WP);
+        WG = ng;
+        WP = np;
     }
-    // Thread composite over its four limbs, earliest first.
-    u32 G = 0, P = 1;
+    if (lane == 0) { wsum_g[warp] = WG; wsum_p[warp] = WP; }
+    __syncthreads();
+    // carry into this warp's first limb when the tile's carry-in is zero
+    u32 cin = 0;
+    for (int w = 0; w < warp; ++w) cin = wsum_g[w] | (wsum_p[w] & cin);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        u32 g = (gm >> t) & 1u, p = (pm >> t) & 1u;
-        compose(g, p, G, P);
-        G = g;
-        P = p;
+    for (int c = 0; c < kChunks; ++c) {
+        const u64 j = j0 + (u64)(warp * 32 * kChunks + c * 32 + lane);
+        const u32 carry = eg[c] | (ep[c] & cin);
+        if (j < out_len) dst[j] = r[c] + carry;
+        cin = cg[c] | (cpp[c] & cin);
     }
-    u32 tg, tp;
-    block_scan_gp(G, P, tg, tp);
-    u32 c = G;  // carry into this thread's first limb when the tile's carry-in is zero
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        const u64 j = j0 + base + t;
-        const u64 v = r[t] + c;
-        c = ((gm >> t) & 1u) | (((pm >> t) & 1u) & c);
-        if (j < out_len) dst[j] = v;
+    if (threadIdx.x == kCrtThreads - 1) {
+        u32 tg = 0, tp = 1;
+        for (int w = 0; w < kCrtThreads / 32; ++w) {
+            u32 g = wsum_g[w], p = wsum_p[w];
+            compose(g, p, tg, tp);
+            tg = g;
+            tp = p;
+        }
+        agg[blockIdx.x] = (uint8_t)(tg | (tp << 1));
     }
-    if (threadIdx.x == 0) agg[blockIdx.x] = (uint8_t)(tg | (tp << 1));
 }
 
-// Resolves the carry into every tile: cin[t] = carry out of tiles 0..t-1.
-__global__ void __launch_bounds__(1024) k_carry_scan(const uint8_t* __restrict__ agg, uint8_t* __restrict__ cin,
-                                                     int tiles) {
+// One CTA: resolves the carry into every tile (cin[t] = carry out of tiles
+// 0..t-1), then adds it. A tile with carry-in one is incremented at its first
+// limb that is not all ones; the all-ones limbs below it become zero. Warps take
+// such tiles in turn; random operands almost never produce one.
+__global__ void __launch_bounds__(1024) k_carry(const uint8_t* __restrict__ agg, uint8_t* __restrict__ cin,
+                                                int tiles, u64* __restrict__ dst, u64 out_len) {
     const int per = (tiles + blockDim.x - 1) / blockDim.x;
     const int t0 = threadIdx.x * per;
     u32 G = 0, P = 1;
@@ -204,26 +236,23 @@ __global__ void __launch_bounds__(1024) k_carry_scan(const uint8_t* __restrict__
         cin[t] = (uint8_t)c;
         c = (agg[t] & 1u) | (((agg[t] >> 1) & 1u) & c);
     }
-}
-
-// Adds a carry of one into each tile that receives it.
-__global__ void __launch_bounds__(kCrtThreads) k_carry_apply(u64* __restrict__ dst, u64 out_len,
-                                                              const uint8_t* __restrict__ cin) {
-    if (!cin[blockIdx.x]) return;
-    __shared__ unsigned long long first;
-    const u64 j0 = (u64)blockIdx.x * kCrtTile;
-    const u64 end = min(j0 + (u64)kCrtTile, out_len);
-    if (threadIdx.x == 0) first = end;
     __syncthreads();
-    unsigned long long mine = end;
-    for (u64 j = j0 + threadIdx.x; j < end; j += blockDim.x)
-        if (dst[j] != ~0ull) { mine = j; break; }
-    atomicMin(&first, mine);
-    __syncthreads();
-    const u64 f = first;
-    for (u64 j = j0 + threadIdx.x; j < end; j += blockDim.x) {
-        if (j < f) dst[j] = 0;
-        else if (j == f) dst[j] += 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int t = warp; t < tiles; t += nwarps) {
+        if (!cin[t]) continue;
+        const u64 begin = (u64)t * kCrtTile;
+        const u64 end = min(begin + (u64)kCrtTile, out_len);
+        for (u64 base = begin; base < end; base += 32) {
+            const u64 j = base + lane;
+            const bool ones = j >= end || dst[j] == ~0ull;
+            const unsigned stop = __ballot_sync(0xffffffffu, !ones);
+            const int first = stop ? __ffs(stop) - 1 : 32;
+            if (j < end) {
+                if (lane < first) dst[j] = 0;
+                else if (lane == first) dst[j] += 1;
+            }
+            if (stop) break;
+        }
     }
 }
 
@@ -277,9 +306,7 @@ static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u
     const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
     k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst, agg, cp);
     if (mark) mark(st);
-    k_carry_scan<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles);
-    if (mark) mark(st);
-    k_carry_apply<<<tiles, kCrtThreads, 0, st>>>(dst, out_len, agg + tiles);
+    k_carry<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles, dst, out_len);
     if (mark) mark(st);
 }
 

@@ -3,10 +3,15 @@
 // The reference runs radix-2/4/8/16 stages over remainder trees with 16-point
 // register leaves (src/transform/forward.rs:200-298, src/transform/stage.rs:34-175,
 // src/arch/schedule/leaf.rs:28-82). Here one CTA transforms one or more vectors of
-// n = 2^log_n points held in shared memory. Each thread loads 2^RB points spaced
-// `hq` apart into registers, runs RB butterfly levels there, and stores them back,
+// n = 2^LOG_N points held in shared memory. Each thread loads 2^RB points spaced
+// HQ apart into registers, runs RB butterfly levels there, and stores them back,
 // so shared memory is touched twice per RB levels. Roots come from level-major
 // tables (entry h + j holds w_{2h}^{+-j}), read through the read-only cache.
+//
+// Every size is a template parameter, so the slot of point m of a register block
+// is the block's base plus a compile-time offset and each twiddle load has an
+// immediate offset from one per-block base: the only per-point instructions left
+// are the loads, the stores and the butterflies themselves.
 //
 // Forward: decimation in frequency, natural order in, bit-reversed order out.
 // Inverse: decimation in time, bit-reversed order in, natural order out.
@@ -14,114 +19,113 @@
 #include "ntt_arith.cuh"
 
 // Shared-memory slot of logical index i: one pad word per 32 words.
-__device__ __forceinline__ int pad_index(int i) { return i + (i >> 5); }
+__host__ __device__ constexpr int pad_index(int i) { return i + (i >> 5); }
 
 // Padded words that hold one vector of n points.
-__host__ __device__ inline int padded_len(int n) { return n + (n >> 5); }
+__host__ __device__ constexpr int padded_len(int n) { return n + (n >> 5); }
 
-template <class A, int RB>
-__device__ __forceinline__ void dif_pass(u32* __restrict__ s, int log_n, int level, int nvec,
-                                         int vstride, const uint2* __restrict__ tw, u32 p) {
+// For a register block of 2^RB points spaced S apart whose first point i0 satisfies
+// i0 mod 32 + (2^RB - 1) * S < 32 whenever 2^RB * S <= 32 (blocks are aligned), the
+// slot of point m is pad_index(i0) + m*S + ((m*S) >> 5).
+template <int S>
+__device__ __forceinline__ constexpr int slot_offset(int m) {
+    return m * S + ((m * S) >> 5);
+}
+
+template <class A, int LOG_N, int LEVEL, int RB, int NT>
+__device__ __forceinline__ void dif_pass(u32* __restrict__ s, int nvec, int vstride, const uint2* __restrict__ tw,
+                                         u32 p) {
     constexpr int E = 1 << RB;
-    const int log_hq = log_n - level - RB;
-    const int hq = 1 << log_hq;
-    const int log_gpv = log_n - RB;
-    const int total = nvec << log_gpv;
-    for (int g = threadIdx.x; g < total; g += blockDim.x) {
-        const int v = g >> log_gpv;
-        const int gg = g & ((1 << log_gpv) - 1);
-        const int j0 = gg & (hq - 1);
-        const int i0 = ((gg >> log_hq) << (log_hq + RB)) + j0;
-        u32* base = s + v * vstride;
+    constexpr int LOG_HQ = LOG_N - LEVEL - RB;
+    constexpr int HQ = 1 << LOG_HQ;
+    constexpr int LOG_GPV = LOG_N - RB;
+    const int total = nvec << LOG_GPV;
+#pragma unroll 1
+    for (int g = threadIdx.x; g < total; g += NT) {
+        const int v = g >> LOG_GPV;
+        const int gg = g & ((1 << LOG_GPV) - 1);
+        const int j0 = gg & (HQ - 1);
+        const int i0 = ((gg >> LOG_HQ) << (LOG_HQ + RB)) + j0;
+        u32* base = s + v * vstride + pad_index(i0);
+        const uint2* twb = tw + j0;
         u32 x[E];
 #pragma unroll
-        for (int m = 0; m < E; ++m) x[m] = base[pad_index(i0 + m * hq)];
+        for (int m = 0; m < E; ++m) x[m] = base[slot_offset<HQ>(m)];
 #pragma unroll
         for (int t = 0; t < RB; ++t) {
             const int half = E >> (t + 1);
-            const int hl = hq * half;
 #pragma unroll
-            for (int m = 0; m < E; ++m) {
-                if ((m & half) == 0) {
-                    const int j = j0 + (m & (half - 1)) * hq;
-                    const uint2 w = __ldg(tw + hl + j);
-                    A::dif(x[m], x[m + half], w, p);
-                }
+            for (int c = 0; c < half; ++c) {
+                // butterflies (m, m + half) with m = blk*2*half + c share twiddle c
+                const uint2 w = __ldg(twb + HQ * half + c * HQ);
+#pragma unroll
+                for (int b = 0; b < E; b += 2 * half) A::dif(x[b + c], x[b + c + half], w, p);
             }
         }
 #pragma unroll
-        for (int m = 0; m < E; ++m) base[pad_index(i0 + m * hq)] = x[m];
+        for (int m = 0; m < E; ++m) base[slot_offset<HQ>(m)] = x[m];
     }
 }
 
-template <class A, int RB>
-__device__ __forceinline__ void dit_pass(u32* __restrict__ s, int log_n, int level, int nvec,
-                                         int vstride, const uint2* __restrict__ tw, u32 p) {
+template <class A, int LOG_N, int LEVEL, int RB, int NT>
+__device__ __forceinline__ void dit_pass(u32* __restrict__ s, int nvec, int vstride, const uint2* __restrict__ tw,
+                                         u32 p) {
     constexpr int E = 1 << RB;
-    const int hs = 1 << level;
-    const int log_gpv = log_n - RB;
-    const int total = nvec << log_gpv;
-    for (int g = threadIdx.x; g < total; g += blockDim.x) {
-        const int v = g >> log_gpv;
-        const int gg = g & ((1 << log_gpv) - 1);
-        const int j0 = gg & (hs - 1);
-        const int i0 = ((gg >> level) << (level + RB)) + j0;
-        u32* base = s + v * vstride;
+    constexpr int HS = 1 << LEVEL;
+    constexpr int LOG_GPV = LOG_N - RB;
+    const int total = nvec << LOG_GPV;
+#pragma unroll 1
+    for (int g = threadIdx.x; g < total; g += NT) {
+        const int v = g >> LOG_GPV;
+        const int gg = g & ((1 << LOG_GPV) - 1);
+        const int j0 = gg & (HS - 1);
+        const int i0 = ((gg >> LEVEL) << (LEVEL + RB)) + j0;
+        u32* base = s + v * vstride + pad_index(i0);
+        const uint2* twb = tw + j0;
         u32 x[E];
 #pragma unroll
-        for (int m = 0; m < E; ++m) x[m] = base[pad_index(i0 + m * hs)];
+        for (int m = 0; m < E; ++m) x[m] = base[slot_offset<HS>(m)];
 #pragma unroll
         for (int t = 0; t < RB; ++t) {
             const int dist = 1 << t;
-            const int h = hs << t;
 #pragma unroll
-            for (int m = 0; m < E; ++m) {
-                if ((m & dist) == 0) {
-                    const int j = j0 + (m & (dist - 1)) * hs;
-                    const uint2 w = __ldg(tw + h + j);
-                    A::dit(x[m], x[m + dist], w, p);
-                }
+            for (int c = 0; c < dist; ++c) {
+                const uint2 w = __ldg(twb + (HS << t) + c * HS);
+#pragma unroll
+                for (int b = 0; b < E; b += 2 * dist) A::dit(x[b + c], x[b + c + dist], w, p);
             }
         }
 #pragma unroll
-        for (int m = 0; m < E; ++m) base[pad_index(i0 + m * hs)] = x[m];
+        for (int m = 0; m < E; ++m) base[slot_offset<HS>(m)] = x[m];
     }
 }
 
-// Full forward transform of nvec vectors; ends with a barrier.
-template <class A>
-__device__ __forceinline__ void dif_full(u32* s, int log_n, int nvec, int vstride,
-                                         const uint2* tw, u32 p) {
-    int level = 0;
-    while (log_n - level >= 4) {
-        dif_pass<A, 4>(s, log_n, level, nvec, vstride, tw, p);
-        level += 4;
+// Full forward transform of nvec vectors of 2^LOG_N points; ends with a barrier.
+template <class A, int LOG_N, int NT, int LEVEL = 0>
+__device__ __forceinline__ void dif_full(u32* s, int nvec, int vstride, const uint2* tw, u32 p) {
+    if constexpr (LOG_N - LEVEL >= 4) {
+        dif_pass<A, LOG_N, LEVEL, 4, NT>(s, nvec, vstride, tw, p);
+        __syncthreads();
+        dif_full<A, LOG_N, NT, LEVEL + 4>(s, nvec, vstride, tw, p);
+    } else if constexpr (LOG_N - LEVEL > 0) {
+        dif_pass<A, LOG_N, LEVEL, LOG_N - LEVEL, NT>(s, nvec, vstride, tw, p);
         __syncthreads();
     }
-    switch (log_n - level) {
-        case 1: dif_pass<A, 1>(s, log_n, level, nvec, vstride, tw, p); break;
-        case 2: dif_pass<A, 2>(s, log_n, level, nvec, vstride, tw, p); break;
-        case 3: dif_pass<A, 3>(s, log_n, level, nvec, vstride, tw, p); break;
-        default: break;
-    }
-    __syncthreads();
 }
 
-// Full inverse transform (unscaled) of nvec vectors; ends with a barrier.
-template <class A>
-__device__ __forceinline__ void dit_full(u32* s, int log_n, int nvec, int vstride,
-                                         const uint2* tw, u32 p) {
-    int level = 0;
-    switch (log_n & 3) {
-        case 1: dit_pass<A, 1>(s, log_n, 0, nvec, vstride, tw, p); level = 1; break;
-        case 2: dit_pass<A, 2>(s, log_n, 0, nvec, vstride, tw, p); level = 2; break;
-        case 3: dit_pass<A, 3>(s, log_n, 0, nvec, vstride, tw, p); level = 3; break;
-        default: break;
-    }
-    if (level) __syncthreads();
-    while (level < log_n) {
-        dit_pass<A, 4>(s, log_n, level, nvec, vstride, tw, p);
-        level += 4;
+// Full inverse transform (unscaled); the short pass runs first. Ends with a barrier.
+template <class A, int LOG_N, int NT, int LEVEL = -1>
+__device__ __forceinline__ void dit_full(u32* s, int nvec, int vstride, const uint2* tw, u32 p) {
+    if constexpr (LEVEL < 0) {
+        constexpr int R0 = LOG_N & 3;
+        if constexpr (R0 > 0) {
+            dit_pass<A, LOG_N, 0, R0, NT>(s, nvec, vstride, tw, p);
+            __syncthreads();
+        }
+        dit_full<A, LOG_N, NT, R0>(s, nvec, vstride, tw, p);
+    } else if constexpr (LEVEL < LOG_N) {
+        dit_pass<A, LOG_N, LEVEL, 4, NT>(s, nvec, vstride, tw, p);
         __syncthreads();
+        dit_full<A, LOG_N, NT, LEVEL + 4>(s, nvec, vstride, tw, p);
     }
 }

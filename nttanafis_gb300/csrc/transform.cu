@@ -14,6 +14,8 @@
 //    k_inv_cols (column DIT + canonical residues). The spectrum order between the
 //    passes is the four-step's transposed, bit-reversed order; only the inverse
 //    reads it, so no transpose is ever materialised.
+// Every kernel is instantiated per transform size so all shared-memory strides are
+// compile-time constants.
 #include "launch.h"
 #include "ntt_passes.cuh"
 
@@ -21,92 +23,119 @@ namespace ntt {
 
 constexpr int kThreads = 256;
 
+// log2 of the columns one CTA of a column pass owns: 2^14 points per CTA, at
+// least 8 columns (32-byte row segments of u32), at most 32.
+__host__ __device__ constexpr int col_group_log(int log_r) {
+    return 14 - log_r < 3 ? 3 : (14 - log_r > 5 ? 5 : 14 - log_r);
+}
+// Padded words per column in shared memory: congruent to 32/G mod 32 so that a
+// warp's G columns times 32/G rows fall in distinct banks.
+__host__ __device__ constexpr int col_vstride(int log_r) {
+    return padded_len(1 << log_r) +
+           ((((32 >> col_group_log(log_r)) - padded_len(1 << log_r)) % 32) + 32) % 32;
+}
+
 template <class A, bool SIGNED>
-__device__ __forceinline__ u32 load_coefficient(const u64* __restrict__ src, u64 idx, u64 len,
-                                                const PrimeParams& pp) {
-    if (idx >= len) return 0;
-    const u64 x = __ldg(src + idx);
+__device__ __forceinline__ u32 reduce_coefficient(u64 x, const PrimeParams& pp) {
     return SIGNED ? reduce_signed<A>(x, pp) : reduce_limb<A>(x, pp);
 }
 
 // One CTA transforms one prime: pack, forward a (and b), pointwise, inverse, scale.
-template <class A, bool SQUARE, bool SIGNED>
+template <class A, bool SQUARE, bool SIGNED, int LOG_N>
 __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
+    constexpr int N = 1 << LOG_N;
+    constexpr int VS = padded_len(N);
     const PrimeParams& pp = g.ps.pr[blockIdx.x];
-    const int n = 1 << g.log_t;
-    const int vs = padded_len(n);
     u32* sa = sm;
-    u32* sb = sm + vs;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        sa[pad_index(i)] = load_coefficient<A, SIGNED>(g.a, (u64)i, g.la, pp);
-        if (!SQUARE) sb[pad_index(i)] = load_coefficient<A, SIGNED>(g.b, (u64)i, g.lb, pp);
+    u32* sb = sm + VS;
+    for (int i = threadIdx.x; i < N; i += kThreads) {
+        sa[pad_index(i)] = (u64)i < g.la ? reduce_coefficient<A, SIGNED>(__ldg(g.a + i), pp) : 0u;
+        if (!SQUARE) sb[pad_index(i)] = (u64)i < g.lb ? reduce_coefficient<A, SIGNED>(__ldg(g.b + i), pp) : 0u;
     }
     __syncthreads();
-    dif_full<A>(sm, g.log_t, SQUARE ? 1 : 2, vs, pp.fwd, pp.p);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    dif_full<A, LOG_N, kThreads>(sm, SQUARE ? 1 : 2, VS, pp.fwd, pp.p);
+    for (int i = threadIdx.x; i < N; i += kThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
         const u32 y = SQUARE ? x : sb[k];
         sa[k] = A::mulc(A::pointwise(x, y, pp.p, pp.pni), pp.scale, pp.p);
     }
     __syncthreads();
-    dit_full<A>(sa, g.log_t, 1, vs, pp.inv, pp.p);
-    u32* out = g.spec + ((size_t)blockIdx.x << g.log_t);
-    for (int i = threadIdx.x; i < (int)g.conv_len; i += blockDim.x)
-        out[i] = A::canonical(sa[pad_index(i)], pp.p);
+    dit_full<A, LOG_N, kThreads>(sa, 1, VS, pp.inv, pp.p);
+    u32* out = g.spec + ((size_t)blockIdx.x << LOG_N);
+    for (int i = threadIdx.x; i < (int)g.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
 }
 
-// Column pass of the forward four-step: G columns of R points per CTA.
+// Column pass of the forward four-step: G columns of R = 2^LOG_R points per CTA.
 // grid = (C / G, np, operands). Coefficient n = n1*C + n2 sits at row n1, column n2.
-template <class A, bool SIGNED>
+template <class A, bool SIGNED, int LOG_R>
 __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
+    constexpr int LOG_G = col_group_log(LOG_R);
+    constexpr int G = 1 << LOG_G;
+    constexpr int VS = col_vstride(LOG_R);
+    constexpr int COUNT = G << LOG_R;
+    constexpr int BATCH = 8;
     const int prime = blockIdx.y;
     const int op = blockIdx.z;
     const PrimeParams& pp = g.ps.pr[prime];
-    const u64* src = op ? g.b : g.a;
+    const u64* __restrict__ src = op ? g.b : g.a;
     const u64 len = op ? g.lb : g.la;
-    const int G = 1 << g.log_g;
-    const int col0 = blockIdx.x << g.log_g;
-    const int count = 1 << (g.log_r + g.log_g);
-    for (int e = threadIdx.x; e < count; e += blockDim.x) {
-        const int c = e & (G - 1);
-        const int r = e >> g.log_g;
-        const u64 idx = ((u64)r << g.log_c) + (u64)(col0 + c);
-        sm[c * g.vstride_col + pad_index(r)] = load_coefficient<A, SIGNED>(src, idx, len, pp);
+    const int log_c = g.log_c;
+    const int col0 = blockIdx.x << LOG_G;
+    // Rows at or past len/C are zero: only rows below `rows` are read.
+    const u64 rows = (len + ((u64)1 << log_c) - 1) >> log_c;
+    const int live = rows < ((u64)1 << LOG_R) ? (int)rows << LOG_G : COUNT;
+    for (int e0 = 0; e0 < COUNT; e0 += kThreads * BATCH) {
+        u64 x[BATCH];
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = e0 + u * kThreads + threadIdx.x;
+            const u64 idx = ((u64)(e >> LOG_G) << log_c) + (u64)(col0 + (e & (G - 1)));
+            x[u] = (e < live && idx < len) ? __ldg(src + idx) : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = e0 + u * kThreads + threadIdx.x;
+            if (e < COUNT) {
+                const u32 r = (e < live && x[u]) ? reduce_coefficient<A, SIGNED>(x[u], pp) : 0u;
+                sm[(e & (G - 1)) * VS + pad_index(e >> LOG_G)] = r;
+            }
+        }
     }
     __syncthreads();
-    dif_full<A>(sm, g.log_r, G, g.vstride_col, pp.fwd, pp.p);
+    dif_full<A, LOG_R, kThreads>(sm, G, VS, pp.fwd, pp.p);
     u32* dst = g.spec + ((size_t)(op * g.np + prime) << g.log_t);
     const u32 lo_mask = (1u << g.s_bits) - 1;
-    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+    for (int e = threadIdx.x; e < COUNT; e += kThreads) {
         const int c = e & (G - 1);
-        const int j = e >> g.log_g;
-        u32 x = sm[c * g.vstride_col + pad_index(j)];
-        const u32 ex = (u32)(col0 + c) * (__brev((u32)j) >> (32 - g.log_r));
+        const int j = e >> LOG_G;
+        u32 x = sm[c * VS + pad_index(j)];
+        const u32 ex = (u32)(col0 + c) * (__brev((u32)j) >> (32 - LOG_R));
         x = A::mulc(x, __ldg(pp.f4_lo + (ex & lo_mask)), pp.p);
         x = A::mulc(x, __ldg(pp.f4_hi + (ex >> g.s_bits)), pp.p);
-        dst[((size_t)j << g.log_c) + col0 + c] = x;
+        dst[((size_t)j << log_c) + col0 + c] = x;
     }
 }
 
 // Row pass: forward rows of a (and b), pointwise product, inverse rows, inverse
 // four-step twiddle with the 2^32 / T scale. grid = (R, np); writes over a's rows.
-template <class A, bool SQUARE>
+template <class A, bool SQUARE, int LOG_C>
 __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
+    constexpr int C = 1 << LOG_C;
+    constexpr int VS = padded_len(C);
     const int prime = blockIdx.y;
     const int row = blockIdx.x;
     const PrimeParams& pp = g.ps.pr[prime];
-    const int C = 1 << g.log_c;
-    const int vs = padded_len(C);
-    uint4* ra = reinterpret_cast<uint4*>(g.spec + ((size_t)prime << g.log_t) + ((size_t)row << g.log_c));
+    uint4* ra = reinterpret_cast<uint4*>(g.spec + ((size_t)prime << g.log_t) + ((size_t)row << LOG_C));
     const uint4* rb = reinterpret_cast<const uint4*>(
-        g.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << g.log_c));
+        g.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C));
     u32* sa = sm;
-    u32* sb = sm + vs;
-    for (int q = threadIdx.x; q < (C >> 2); q += blockDim.x) {
+    u32* sb = sm + VS;
+#pragma unroll 4
+    for (int q = threadIdx.x; q < (C >> 2); q += kThreads) {
         const int k = pad_index(q << 2);
         const uint4 v = ra[q];
         sa[k] = v.x; sa[k + 1] = v.y; sa[k + 2] = v.z; sa[k + 3] = v.w;
@@ -116,23 +145,24 @@ __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ Trans
         }
     }
     __syncthreads();
-    dif_full<A>(sm, g.log_c, SQUARE ? 1 : 2, vs, pp.fwd, pp.p);
-    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+    dif_full<A, LOG_C, kThreads>(sm, SQUARE ? 1 : 2, VS, pp.fwd, pp.p);
+    for (int i = threadIdx.x; i < C; i += kThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
         sa[k] = A::pointwise(x, SQUARE ? x : sb[k], pp.p, pp.pni);
     }
     __syncthreads();
-    dit_full<A>(sa, g.log_c, 1, vs, pp.inv, pp.p);
+    dit_full<A, LOG_C, kThreads>(sa, 1, VS, pp.inv, pp.p);
     const u32 rowexp = __brev((u32)row) >> (32 - g.log_r);
     const u32 lo_mask = (1u << g.s_bits) - 1;
-    for (int q = threadIdx.x; q < (C >> 2); q += blockDim.x) {
+#pragma unroll 4
+    for (int q = threadIdx.x; q < (C >> 2); q += kThreads) {
         const int k = pad_index(q << 2);
         u32 v[4];
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const u32 ex = (u32)((q << 2) + t) * rowexp;
-            u32 x = A::mulc(sa[k + t], __ldg(pp.i4_lo + (ex & lo_mask)), pp.p);
+            const u32 x = A::mulc(sa[k + t], __ldg(pp.i4_lo + (ex & lo_mask)), pp.p);
             v[t] = A::mulc(x, __ldg(pp.i4_hi + (ex >> g.s_bits)), pp.p);
         }
         ra[q] = make_uint4(v[0], v[1], v[2], v[3]);
@@ -140,124 +170,192 @@ __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ Trans
 }
 
 // Column pass of the inverse four-step: column DIT, canonical residues in place.
-template <class A>
+template <class A, int LOG_R>
 __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
+    constexpr int LOG_G = col_group_log(LOG_R);
+    constexpr int G = 1 << LOG_G;
+    constexpr int VS = col_vstride(LOG_R);
+    constexpr int COUNT = G << LOG_R;
+    constexpr int BATCH = 8;
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
-    const int G = 1 << g.log_g;
-    const int col0 = blockIdx.x << g.log_g;
-    const int count = 1 << (g.log_r + g.log_g);
+    const int log_c = g.log_c;
+    const int col0 = blockIdx.x << LOG_G;
     u32* base = g.spec + ((size_t)prime << g.log_t);
-    for (int e = threadIdx.x; e < count; e += blockDim.x) {
-        const int c = e & (G - 1);
-        const int r = e >> g.log_g;
-        sm[c * g.vstride_col + pad_index(r)] = base[((size_t)r << g.log_c) + col0 + c];
+    for (int e0 = 0; e0 < COUNT; e0 += kThreads * BATCH) {
+        u32 x[BATCH];
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = e0 + u * kThreads + threadIdx.x;
+            x[u] = e < COUNT ? base[((size_t)(e >> LOG_G) << log_c) + col0 + (e & (G - 1))] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int e = e0 + u * kThreads + threadIdx.x;
+            if (e < COUNT) sm[(e & (G - 1)) * VS + pad_index(e >> LOG_G)] = x[u];
+        }
     }
     __syncthreads();
-    dit_full<A>(sm, g.log_r, G, g.vstride_col, pp.inv, pp.p);
-    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+    dit_full<A, LOG_R, kThreads>(sm, G, VS, pp.inv, pp.p);
+    for (int e = threadIdx.x; e < COUNT; e += kThreads) {
         const int c = e & (G - 1);
-        const int r = e >> g.log_g;
-        base[((size_t)r << g.log_c) + col0 + c] = A::canonical(sm[c * g.vstride_col + pad_index(r)], pp.p);
+        const int r = e >> LOG_G;
+        base[((size_t)r << log_c) + col0 + c] = A::canonical(sm[c * VS + pad_index(r)], pp.p);
     }
 }
 
 // ---------------------------------------------------------------------------------
-// Launchers
+// Launchers: one instantiation per transform size. The lazy arithmetic covers
+// T <= 2^23 (one-CTA sizes 2^4..2^13, columns 2^7..2^11, rows 2^7..2^12); the wide
+// arithmetic covers T = 2^24, 2^25 (columns 2^12, rows 2^12..2^13).
 
-static size_t small_smem(const TransformArgs& g, bool square) {
-    return (size_t)(square ? 1 : 2) * padded_len(1 << g.log_t) * sizeof(u32);
-}
-static size_t col_smem(const TransformArgs& g) {
-    return (size_t)g.vstride_col * (1u << g.log_g) * sizeof(u32);
-}
-static size_t row_smem(const TransformArgs& g, bool square) {
-    return (size_t)(square ? 1 : 2) * padded_len(1 << g.log_c) * sizeof(u32);
+constexpr int kSmemOptIn = 200 * 1024;
+
+template <class K>
+static cudaError_t opt_in(K kernel) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn);
 }
 
-template <class A>
-static cudaError_t small_for(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
-    const dim3 grid(g.np);
-    const size_t sm = small_smem(g, square);
-    if (square) {
-        if (sign) k_small<A, true, true><<<grid, kThreads, sm, st>>>(g);
-        else k_small<A, true, false><<<grid, kThreads, sm, st>>>(g);
-    } else {
-        if (sign) k_small<A, false, true><<<grid, kThreads, sm, st>>>(g);
-        else k_small<A, false, false><<<grid, kThreads, sm, st>>>(g);
-    }
+template <class A, int L>
+static cudaError_t small_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
+    auto k = square ? (sign ? k_small<A, true, true, L> : k_small<A, true, false, L>)
+                    : (sign ? k_small<A, false, true, L> : k_small<A, false, false, L>);
+    if (init) return opt_in(k);
+    const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
+    k<<<g.np, kThreads, smem, st>>>(g);
     return cudaGetLastError();
+}
+
+template <class A, int L>
+static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
+    auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
+    if (init) return opt_in(k);
+    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, square ? 1 : 2);
+    const size_t smem = (size_t)col_vstride(L) * (1 << col_group_log(L)) * sizeof(u32);
+    k<<<grid, kThreads, smem, st>>>(g);
+    return cudaGetLastError();
+}
+
+template <class A, int L>
+static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
+    auto k = square ? k_rows<A, true, L> : k_rows<A, false, L>;
+    if (init) return opt_in(k);
+    const dim3 grid(1u << g.log_r, g.np);
+    const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
+    k<<<grid, kThreads, smem, st>>>(g);
+    return cudaGetLastError();
+}
+
+template <class A, int L>
+static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool init) {
+    auto k = k_inv_cols<A, L>;
+    if (init) return opt_in(k);
+    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np);
+    const size_t smem = (size_t)col_vstride(L) * (1 << col_group_log(L)) * sizeof(u32);
+    k<<<grid, kThreads, smem, st>>>(g);
+    return cudaGetLastError();
+}
+
+static cudaError_t small_any(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
+    switch (g.log_t) {
+        case 4: return small_at<LazyArith, 4>(g, square, sign, st, init);
+        case 5: return small_at<LazyArith, 5>(g, square, sign, st, init);
+        case 6: return small_at<LazyArith, 6>(g, square, sign, st, init);
+        case 7: return small_at<LazyArith, 7>(g, square, sign, st, init);
+        case 8: return small_at<LazyArith, 8>(g, square, sign, st, init);
+        case 9: return small_at<LazyArith, 9>(g, square, sign, st, init);
+        case 10: return small_at<LazyArith, 10>(g, square, sign, st, init);
+        case 11: return small_at<LazyArith, 11>(g, square, sign, st, init);
+        case 12: return small_at<LazyArith, 12>(g, square, sign, st, init);
+        case 13: return small_at<LazyArith, 13>(g, square, sign, st, init);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+static cudaError_t fwd_cols_any(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
+    if (g.wide) {
+        if (g.log_r == 12) return fwd_cols_at<WideArith, 12>(g, square, sign, st, init);
+        return cudaErrorInvalidValue;
+    }
+    switch (g.log_r) {
+        case 7: return fwd_cols_at<LazyArith, 7>(g, square, sign, st, init);
+        case 8: return fwd_cols_at<LazyArith, 8>(g, square, sign, st, init);
+        case 9: return fwd_cols_at<LazyArith, 9>(g, square, sign, st, init);
+        case 10: return fwd_cols_at<LazyArith, 10>(g, square, sign, st, init);
+        case 11: return fwd_cols_at<LazyArith, 11>(g, square, sign, st, init);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+static cudaError_t rows_any(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
+    if (g.wide) {
+        if (g.log_c == 12) return rows_at<WideArith, 12>(g, square, st, init);
+        if (g.log_c == 13) return rows_at<WideArith, 13>(g, square, st, init);
+        return cudaErrorInvalidValue;
+    }
+    switch (g.log_c) {
+        case 7: return rows_at<LazyArith, 7>(g, square, st, init);
+        case 8: return rows_at<LazyArith, 8>(g, square, st, init);
+        case 9: return rows_at<LazyArith, 9>(g, square, st, init);
+        case 10: return rows_at<LazyArith, 10>(g, square, st, init);
+        case 11: return rows_at<LazyArith, 11>(g, square, st, init);
+        case 12: return rows_at<LazyArith, 12>(g, square, st, init);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+static cudaError_t inv_cols_any(const TransformArgs& g, cudaStream_t st, bool init) {
+    if (g.wide) {
+        if (g.log_r == 12) return inv_cols_at<WideArith, 12>(g, st, init);
+        return cudaErrorInvalidValue;
+    }
+    switch (g.log_r) {
+        case 7: return inv_cols_at<LazyArith, 7>(g, st, init);
+        case 8: return inv_cols_at<LazyArith, 8>(g, st, init);
+        case 9: return inv_cols_at<LazyArith, 9>(g, st, init);
+        case 10: return inv_cols_at<LazyArith, 10>(g, st, init);
+        case 11: return inv_cols_at<LazyArith, 11>(g, st, init);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
-    return g.wide ? small_for<WideArith>(g, square, sign, st) : small_for<LazyArith>(g, square, sign, st);
+    return small_any(g, square, sign, st, false);
 }
-
-template <class A>
-static cudaError_t fwd_cols_for(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
-    const dim3 grid(1u << (g.log_c - g.log_g), g.np, square ? 1 : 2);
-    const size_t sm = col_smem(g);
-    if (sign) k_fwd_cols<A, true><<<grid, kThreads, sm, st>>>(g);
-    else k_fwd_cols<A, false><<<grid, kThreads, sm, st>>>(g);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
-    return g.wide ? fwd_cols_for<WideArith>(g, square, sign, st)
-                  : fwd_cols_for<LazyArith>(g, square, sign, st);
+    return fwd_cols_any(g, square, sign, st, false);
 }
-
-template <class A>
-static cudaError_t rows_for(const TransformArgs& g, bool square, cudaStream_t st) {
-    const dim3 grid(1u << g.log_r, g.np);
-    const size_t sm = row_smem(g, square);
-    if (square) k_rows<A, true><<<grid, kThreads, sm, st>>>(g);
-    else k_rows<A, false><<<grid, kThreads, sm, st>>>(g);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st) {
-    return g.wide ? rows_for<WideArith>(g, square, st) : rows_for<LazyArith>(g, square, st);
+    return rows_any(g, square, st, false);
 }
+cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st) { return inv_cols_any(g, st, false); }
 
-template <class A>
-static cudaError_t inv_cols_for(const TransformArgs& g, cudaStream_t st) {
-    const dim3 grid(1u << (g.log_c - g.log_g), g.np);
-    k_inv_cols<A><<<grid, kThreads, col_smem(g), st>>>(g);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st) {
-    return g.wide ? inv_cols_for<WideArith>(g, st) : inv_cols_for<LazyArith>(g, st);
-}
-
-template <class K>
-static cudaError_t opt_in(K kernel, int bytes) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-}
-
-template <class A>
-static cudaError_t init_for() {
-    const int big = 200 * 1024;
-    cudaError_t e = cudaSuccess;
-    auto chk = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
-    chk(opt_in(k_small<A, true, true>, big));
-    chk(opt_in(k_small<A, true, false>, big));
-    chk(opt_in(k_small<A, false, true>, big));
-    chk(opt_in(k_small<A, false, false>, big));
-    chk(opt_in(k_fwd_cols<A, true>, big));
-    chk(opt_in(k_fwd_cols<A, false>, big));
-    chk(opt_in(k_rows<A, true>, big));
-    chk(opt_in(k_rows<A, false>, big));
-    chk(opt_in(k_inv_cols<A>, big));
-    return e;
-}
-
+// Raises the dynamic shared-memory limit of every instantiation (both operand
+// modes) on the current device.
 cudaError_t init_transform_kernels() {
-    cudaError_t e = init_for<LazyArith>();
-    if (e != cudaSuccess) return e;
-    return init_for<WideArith>();
+    cudaError_t e = cudaSuccess;
+    TransformArgs g{};
+    for (int sq = 0; sq < 2; ++sq)
+        for (int sg = 0; sg < 2; ++sg) {
+            for (int l = 4; l <= 13 && e == cudaSuccess; ++l) {
+                g.log_t = l;
+                e = small_any(g, sq, sg, 0, true);
+            }
+            for (int w = 0; w < 2; ++w) {
+                g.wide = w;
+                for (int l = 7; l <= 13 && e == cudaSuccess; ++l) {
+                    g.log_r = l;
+                    g.log_c = l;
+                    const bool col_ok = w ? l == 12 : l <= 11;
+                    const bool row_ok = w ? l >= 12 : l <= 12;
+                    if (col_ok) e = fwd_cols_any(g, sq, sg, 0, true);
+                    if (e == cudaSuccess && row_ok) e = rows_any(g, sq, 0, true);
+                    if (e == cudaSuccess && col_ok) e = inv_cols_any(g, 0, true);
+                }
+            }
+        }
+    return e;
 }
 
 }  // namespace ntt
