@@ -38,35 +38,42 @@ __device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log
         f = fmaf((float)v, cp.pinv[i], f);
     }
     constexpr int MW = NP > 1 ? NP - 1 : 1;  // words of P/p_i
-    u64 acc[NP + 1];
+    // S = sum_i y_i * M_i in NP + 1 words (the top word stays zero), by carry
+    // chains: the low halves of y_i * M_i[w] into word w, the high halves into w+1.
+    u32 S[NP + 1];
 #pragma unroll
-    for (int w = 0; w <= NP; ++w) acc[w] = 0;
+    for (int w = 0; w <= NP; ++w) S[w] = 0;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
+        const u32 yi = y[i];
+        asm volatile("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(S[0]) : "r"(yi), "r"(cp.M[i][0]));
 #pragma unroll
-        for (int w = 0; w < MW; ++w) {
-            const u64 pr = (u64)y[i] * cp.M[i][w];
-            acc[w] += (u32)pr;
-            acc[w + 1] += pr >> 32;
-        }
+        for (int w = 1; w < MW; ++w)
+            asm volatile("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(S[w]) : "r"(yi), "r"(cp.M[i][w]));
+#pragma unroll
+        for (int w = MW; w <= NP; ++w) asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(S[w]));
+        asm volatile("mad.hi.cc.u32 %0, %1, %2, %0;" : "+r"(S[1]) : "r"(yi), "r"(cp.M[i][0]));
+#pragma unroll
+        for (int w = 2; w <= MW; ++w)
+            asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(S[w]) : "r"(yi), "r"(cp.M[i][w - 1]));
+#pragma unroll
+        for (int w = MW + 1; w <= NP; ++w) asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(S[w]));
     }
+    // X = S - q*P in NP + 1 words; the top word is the sign (0 or all ones).
     const u32 q = (u32)(f + cp.bias);
-    u32 x[NP + 1];
-    u64 carry = 0, mul = 0;
-    int64_t borrow = 0;
+    u32 U[NP + 1];
 #pragma unroll
-    for (int w = 0; w < NP; ++w) {
-        const u64 s = acc[w] + carry;
-        carry = s >> 32;
-        mul += (u64)q * cp.P[w];
-        const int64_t d = (int64_t)(u32)s - (int64_t)(u32)mul + borrow;
-        mul >>= 32;
-        x[w] = (u32)d;
-        borrow = d >> 32;  // 0 or -1
-    }
-    // Sign word: S fits NP words, so the result's top is the borrow alone.
-    x[NP] = (u32)borrow;
-    const u64 fill = borrow ? ~0ull : 0ull;
+    for (int w = 0; w < NP; ++w) U[w] = q * cp.P[w];
+    U[NP] = 0;
+    asm volatile("mad.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[1]) : "r"(q), "r"(cp.P[0]));
+#pragma unroll
+    for (int w = 2; w <= NP; ++w)
+        asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[w]) : "r"(q), "r"(cp.P[w - 1]));
+    u32 x[NP + 1];
+    asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(x[0]) : "r"(S[0]), "r"(U[0]));
+#pragma unroll
+    for (int w = 1; w <= NP; ++w) asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(x[w]) : "r"(S[w]), "r"(U[w]));
+    const u64 fill = x[NP] ? ~0ull : 0ull;
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
         const int lo = 2 * w, hi = 2 * w + 1;
@@ -169,12 +176,17 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
     u64 r[kChunks];
     u32 eg[kChunks], ep[kChunks], cg[kChunks], cpp[kChunks];
     u32 WG = 0, WP = 1;  // composite of this warp's chunks so far
+    u32 h_last = 0;      // overflow count of the previous chunk's last limb
+    if (lane == 0) limb_sum(warp * 32 * kChunks - 1, h_last);
+    h_last = __shfl_sync(0xffffffffu, h_last, 0);
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
         const int rel = warp * 32 * kChunks + c * 32 + lane;
-        u32 hprev, h;
-        limb_sum(rel - 1, hprev);
+        u32 h;
         const u64 lo = limb_sum(rel, h);
+        u32 hprev = __shfl_up_sync(0xffffffffu, h, 1);
+        if (lane == 0) hprev = h_last;
+        h_last = __shfl_sync(0xffffffffu, h, 31);
         const u64 s = lo + hprev;
         r[c] = s;
         u32 g = s < lo ? 1u : 0u, p = s == ~0ull ? 1u : 0u;
@@ -220,25 +232,41 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
 // such tiles in turn; random operands almost never produce one.
 __global__ void __launch_bounds__(1024) k_carry(const uint8_t* __restrict__ agg, uint8_t* __restrict__ cin,
                                                 int tiles, u64* __restrict__ dst, u64 out_len) {
+    constexpr int kList = 1024;
+    __shared__ int s_count;
+    __shared__ int s_list[kList];
+    if (threadIdx.x == 0) s_count = 0;
     const int per = (tiles + blockDim.x - 1) / blockDim.x;
     const int t0 = threadIdx.x * per;
+    uint8_t mine[8];  // this thread's aggregates (per <= 8 for up to 8192 tiles)
     u32 G = 0, P = 1;
-    for (int t = t0; t < t0 + per && t < tiles; ++t) {
-        u32 g = agg[t] & 1u, p = (agg[t] >> 1) & 1u;
+    for (int t = t0, i = 0; t < t0 + per && t < tiles; ++t, ++i) {
+        const uint8_t a = agg[t];
+        if (i < 8) mine[i] = a;
+        u32 g = a & 1u, p = (a >> 1) & 1u;
         compose(g, p, G, P);
         G = g;
         P = p;
     }
     u32 tg, tp;
-    block_scan_gp(G, P, tg, tp);
+    block_scan_gp(G, P, tg, tp);  // its barriers also order s_count's initialisation
     u32 c = G;
-    for (int t = t0; t < t0 + per && t < tiles; ++t) {
+    for (int t = t0, i = 0; t < t0 + per && t < tiles; ++t, ++i) {
         cin[t] = (uint8_t)c;
-        c = (agg[t] & 1u) | (((agg[t] >> 1) & 1u) & c);
+        if (c) {
+            const int slot = atomicAdd(&s_count, 1);
+            if (slot < kList) s_list[slot] = t;
+        }
+        const uint8_t a = i < 8 ? mine[i] : agg[t];
+        c = (a & 1u) | (((a >> 1) & 1u) & c);
     }
     __syncthreads();
+    const int count = s_count;
+    if (count == 0) return;  // the usual case: no tile receives a carry
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int t = warp; t < tiles; t += nwarps) {
+    const int work = count <= kList ? count : tiles;
+    for (int i = warp; i < work; i += nwarps) {
+        const int t = count <= kList ? s_list[i] : i;
         if (!cin[t]) continue;
         const u64 begin = (u64)t * kCrtTile;
         const u64 end = min(begin + (u64)kCrtTile, out_len);

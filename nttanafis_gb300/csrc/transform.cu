@@ -69,53 +69,77 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
 
 // Column pass of the forward four-step: G columns of R = 2^LOG_R points per CTA.
 // grid = (C / G, np, operands). Coefficient n = n1*C + n2 sits at row n1, column n2.
+// Column passes map thread t to column c = t mod G and rows r0 + k*RS (r0 = t / G,
+// RS = 256 / G rows per sweep), so global addresses advance by a constant and the
+// shared-memory slot of sweep k is a compile-time offset from the thread's first.
+template <int LOG_R>
+struct ColumnMap {
+    static constexpr int LOG_G = col_group_log(LOG_R);
+    static constexpr int G = 1 << LOG_G;
+    static constexpr int VS = col_vstride(LOG_R);
+    static constexpr int RS = kThreads / G;        // rows per sweep (power of two <= 32)
+    static constexpr int SWEEPS = (1 << LOG_R) / RS;
+    static constexpr int LOG_SW = LOG_R - (8 - LOG_G);
+    __device__ static int col() { return threadIdx.x & (G - 1); }
+    __device__ static int row0() { return threadIdx.x >> LOG_G; }
+    __device__ static int slot0() { return col() * VS + pad_index(row0()); }
+    // bit-reversed row index of sweep k, less that of row0 (the bits are disjoint)
+    __device__ static constexpr u32 brev_sweep(int k) {
+        u32 r = 0;
+        for (int b = 0; b < LOG_SW; ++b) r |= ((u32)(k >> b) & 1u) << (LOG_SW - 1 - b);
+        return r;
+    }
+};
+
 template <class A, bool SIGNED, int LOG_R>
 __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
-    constexpr int LOG_G = col_group_log(LOG_R);
-    constexpr int G = 1 << LOG_G;
-    constexpr int VS = col_vstride(LOG_R);
-    constexpr int COUNT = G << LOG_R;
-    constexpr int BATCH = 8;
+    using M = ColumnMap<LOG_R>;
+    constexpr int B = 8;  // sweeps per batch; B*RS is a multiple of 32, so batch offsets are exact
+    static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
     const int op = blockIdx.z;
     const PrimeParams& pp = g.ps.pr[prime];
     const u64* __restrict__ src = op ? g.b : g.a;
     const u64 len = op ? g.lb : g.la;
     const int log_c = g.log_c;
-    const int col0 = blockIdx.x << LOG_G;
-    // Rows at or past len/C are zero: only rows below `rows` are read.
-    const u64 rows = (len + ((u64)1 << log_c) - 1) >> log_c;
-    const int live = rows < ((u64)1 << LOG_R) ? (int)rows << LOG_G : COUNT;
-    for (int e0 = 0; e0 < COUNT; e0 += kThreads * BATCH) {
-        u64 x[BATCH];
+    const u32 col = (u32)(blockIdx.x << M::LOG_G) + M::col();
+    const int r0 = M::row0();
+    // Sweeps k < live read coefficients; the rest are zero padding.
+    const u64 first = ((u64)r0 << log_c) + col;
+    const u64 step = (u64)M::RS << log_c;
+    const int live = first >= len ? 0 : (int)min((u64)M::SWEEPS, (len - first + step - 1) / step);
+    const u64* __restrict__ p = src + first;
+    u32* s = sm + M::slot0();
+#pragma unroll 1
+    for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
+        u64 x[B];
 #pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const int e = e0 + u * kThreads + threadIdx.x;
-            const u64 idx = ((u64)(e >> LOG_G) << log_c) + (u64)(col0 + (e & (G - 1)));
-            x[u] = (e < live && idx < len) ? __ldg(src + idx) : 0ull;
-        }
+        for (int u = 0; u < B; ++u) x[u] = (k0 + u < live) ? __ldg(p + u * step) : 0ull;
+        p += B * step;
+        u32* sk = s + slot_offset<M::RS>(k0);
 #pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const int e = e0 + u * kThreads + threadIdx.x;
-            if (e < COUNT) {
-                const u32 r = (e < live && x[u]) ? reduce_coefficient<A, SIGNED>(x[u], pp) : 0u;
-                sm[(e & (G - 1)) * VS + pad_index(e >> LOG_G)] = r;
-            }
-        }
+        for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u] ? reduce_coefficient<A, SIGNED>(x[u], pp) : 0u;
     }
     __syncthreads();
-    dif_full<A, LOG_R, kThreads>(sm, G, VS, pp.fwd, pp.p);
-    u32* dst = g.spec + ((size_t)(op * g.np + prime) << g.log_t);
+    dif_full<A, LOG_R, kThreads>(sm, M::G, M::VS, pp.fwd, pp.p);
+    // Four-step twiddle w_T^(col * k1) with k1 = bitrev(row), then the store.
+    u32* dst = g.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
     const u32 lo_mask = (1u << g.s_bits) - 1;
-    for (int e = threadIdx.x; e < COUNT; e += kThreads) {
-        const int c = e & (G - 1);
-        const int j = e >> LOG_G;
-        u32 x = sm[c * VS + pad_index(j)];
-        const u32 ex = (u32)(col0 + c) * (__brev((u32)j) >> (32 - LOG_R));
-        x = A::mulc(x, __ldg(pp.f4_lo + (ex & lo_mask)), pp.p);
-        x = A::mulc(x, __ldg(pp.f4_hi + (ex >> g.s_bits)), pp.p);
-        dst[((size_t)j << log_c) + col0 + c] = x;
+    const u32 e0 = col * (__brev((u32)r0) >> (32 - LOG_R));
+#pragma unroll 1
+    for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
+        const u32 ek = e0 + col * (__brev((u32)k0) >> (32 - M::LOG_SW));
+        const u32* sk = s + slot_offset<M::RS>(k0);
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const u32 ex = ek + col * M::brev_sweep(u);
+            u32 x = sk[slot_offset<M::RS>(u)];
+            x = A::mulc(x, __ldg(pp.f4_lo + (ex & lo_mask)), pp.p);
+            x = A::mulc(x, __ldg(pp.f4_hi + (ex >> g.s_bits)), pp.p);
+            dst[u * step] = x;
+        }
+        dst += B * step;
     }
 }
 
@@ -173,35 +197,35 @@ __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ Trans
 template <class A, int LOG_R>
 __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
-    constexpr int LOG_G = col_group_log(LOG_R);
-    constexpr int G = 1 << LOG_G;
-    constexpr int VS = col_vstride(LOG_R);
-    constexpr int COUNT = G << LOG_R;
-    constexpr int BATCH = 8;
+    using M = ColumnMap<LOG_R>;
+    constexpr int B = 8;
+    static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
-    const int log_c = g.log_c;
-    const int col0 = blockIdx.x << LOG_G;
-    u32* base = g.spec + ((size_t)prime << g.log_t);
-    for (int e0 = 0; e0 < COUNT; e0 += kThreads * BATCH) {
-        u32 x[BATCH];
+    const u64 step = (u64)M::RS << g.log_c;
+    u32* const base = g.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
+                      (blockIdx.x << M::LOG_G) + M::col();
+    u32* s = sm + M::slot0();
+    u32* q = base;
+#pragma unroll 1
+    for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
+        u32 x[B];
 #pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const int e = e0 + u * kThreads + threadIdx.x;
-            x[u] = e < COUNT ? base[((size_t)(e >> LOG_G) << log_c) + col0 + (e & (G - 1))] : 0u;
-        }
+        for (int u = 0; u < B; ++u) x[u] = q[u * step];
+        q += B * step;
+        u32* sk = s + slot_offset<M::RS>(k0);
 #pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const int e = e0 + u * kThreads + threadIdx.x;
-            if (e < COUNT) sm[(e & (G - 1)) * VS + pad_index(e >> LOG_G)] = x[u];
-        }
+        for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u];
     }
     __syncthreads();
-    dit_full<A, LOG_R, kThreads>(sm, G, VS, pp.inv, pp.p);
-    for (int e = threadIdx.x; e < COUNT; e += kThreads) {
-        const int c = e & (G - 1);
-        const int r = e >> LOG_G;
-        base[((size_t)r << log_c) + col0 + c] = A::canonical(sm[c * VS + pad_index(r)], pp.p);
+    dit_full<A, LOG_R, kThreads>(sm, M::G, M::VS, pp.inv, pp.p);
+    q = base;
+#pragma unroll 1
+    for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
+        const u32* sk = s + slot_offset<M::RS>(k0);
+#pragma unroll
+        for (int u = 0; u < B; ++u) q[u * step] = A::canonical(sk[slot_offset<M::RS>(u)], pp.p);
+        q += B * step;
     }
 }
 
