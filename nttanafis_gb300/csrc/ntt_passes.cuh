@@ -6,7 +6,7 @@
 // n = 2^LOG_N points held in shared memory. Each thread loads 2^RB points spaced
 // HQ apart into registers, runs RB butterfly levels there, and stores them back,
 // so shared memory is touched twice per RB levels. Roots come from level-major
-// tables (entry h + j holds w_{2h}^{+-j}), read through the read-only cache.
+// tables (entry h + j holds w_{2h}^{+-j}), in shared memory or global memory.
 //
 // Every size is a template parameter, so the slot of point m of a register block
 // is the block's base plus a compile-time offset and each twiddle load has an
@@ -57,7 +57,7 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, int nvec, int vstr
 #pragma unroll
             for (int c = 0; c < half; ++c) {
                 // butterflies (m, m + half) with m = blk*2*half + c share twiddle c
-                const uint2 w = __ldg(twb + HQ * half + c * HQ);
+                const uint2 w = twb[HQ * half + c * HQ];
 #pragma unroll
                 for (int b = 0; b < E; b += 2 * half) A::dif(x[b + c], x[b + c + half], w, p);
             }
@@ -90,7 +90,7 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, int nvec, int vstr
             const int dist = 1 << t;
 #pragma unroll
             for (int c = 0; c < dist; ++c) {
-                const uint2 w = __ldg(twb + (HS << t) + c * HS);
+                const uint2 w = twb[(HS << t) + c * HS];
 #pragma unroll
                 for (int b = 0; b < E; b += 2 * dist) A::dit(x[b + c], x[b + c + dist], w, p);
             }

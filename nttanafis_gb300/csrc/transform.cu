@@ -23,11 +23,9 @@ namespace ntt {
 
 constexpr int kThreads = 256;
 
-// log2 of the columns one CTA of a column pass owns: 2^14 points per CTA, at
-// least 8 columns (32-byte row segments of u32), at most 32.
-__host__ __device__ constexpr int col_group_log(int log_r) {
-    return 14 - log_r < 3 ? 3 : (14 - log_r > 5 ? 5 : 14 - log_r);
-}
+// log2 of the columns one CTA of a column pass owns: 8 columns, so a row segment
+// is one 32-byte sector of u32 residues (two of u64 limbs).
+__host__ __device__ constexpr int col_group_log(int) { return 3; }
 // Padded words per column in shared memory: congruent to 32/G mod 32 so that a
 // warp's G columns times 32/G rows fall in distinct banks.
 __host__ __device__ constexpr int col_vstride(int log_r) {
@@ -65,6 +63,15 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     dit_full<A, LOG_N, kThreads>(sa, 1, VS, pp.inv, pp.p);
     u32* out = g.spec + ((size_t)blockIdx.x << LOG_N);
     for (int i = threadIdx.x; i < (int)g.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
+}
+
+// Copies the level-major root table of a 2^LOG_N-point transform (entries below
+// 2^LOG_N) into shared memory; the caller's barrier publishes it.
+template <int LOG_N>
+__device__ __forceinline__ void load_table(uint2* dst, const uint2* __restrict__ src) {
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int i = threadIdx.x; i < (1 << LOG_N) / 2; i += kThreads) d4[i] = __ldg(s4 + i);
 }
 
 // Column pass of the forward four-step: G columns of R = 2^LOG_R points per CTA.
@@ -111,18 +118,20 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
     const int live = first >= len ? 0 : (int)min((u64)M::SWEEPS, (len - first + step - 1) / step);
     const u64* __restrict__ p = src + first;
     u32* s = sm + M::slot0();
+    uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
+    load_table<LOG_R>(tw, pp.fwd);
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
         u64 x[B];
 #pragma unroll
-        for (int u = 0; u < B; ++u) x[u] = (k0 + u < live) ? __ldg(p + u * step) : 0ull;
+        for (int u = 0; u < B; ++u) x[u] = (k0 + u < live) ? __ldcs(p + u * step) : 0ull;
         p += B * step;
         u32* sk = s + slot_offset<M::RS>(k0);
 #pragma unroll
         for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u] ? reduce_coefficient<A, SIGNED>(x[u], pp) : 0u;
     }
     __syncthreads();
-    dif_full<A, LOG_R, kThreads>(sm, M::G, M::VS, pp.fwd, pp.p);
+    dif_full<A, LOG_R, kThreads>(sm, M::G, M::VS, tw, pp.p);
     // Four-step twiddle w_T^(col * k1) with k1 = bitrev(row), then the store.
     u32* dst = g.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
     const u32 lo_mask = (1u << g.s_bits) - 1;
@@ -161,10 +170,10 @@ __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ Trans
 #pragma unroll 4
     for (int q = threadIdx.x; q < (C >> 2); q += kThreads) {
         const int k = pad_index(q << 2);
-        const uint4 v = ra[q];
+        const uint4 v = __ldcs(ra + q);
         sa[k] = v.x; sa[k + 1] = v.y; sa[k + 2] = v.z; sa[k + 3] = v.w;
         if (!SQUARE) {
-            const uint4 w = rb[q];
+            const uint4 w = __ldcs(rb + q);
             sb[k] = w.x; sb[k + 1] = w.y; sb[k + 2] = w.z; sb[k + 3] = w.w;
         }
     }
@@ -206,19 +215,21 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ T
     u32* const base = g.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
                       (blockIdx.x << M::LOG_G) + M::col();
     u32* s = sm + M::slot0();
+    uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
+    load_table<LOG_R>(tw, pp.inv);
     u32* q = base;
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
         u32 x[B];
 #pragma unroll
-        for (int u = 0; u < B; ++u) x[u] = q[u * step];
+        for (int u = 0; u < B; ++u) x[u] = __ldcs(q + u * step);
         q += B * step;
         u32* sk = s + slot_offset<M::RS>(k0);
 #pragma unroll
         for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u];
     }
     __syncthreads();
-    dit_full<A, LOG_R, kThreads>(sm, M::G, M::VS, pp.inv, pp.p);
+    dit_full<A, LOG_R, kThreads>(sm, M::G, M::VS, tw, pp.p);
     q = base;
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
@@ -235,6 +246,12 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ T
 // arithmetic covers T = 2^24, 2^25 (columns 2^12, rows 2^12..2^13).
 
 constexpr int kSmemOptIn = 200 * 1024;
+
+// Column residues plus the level root table (8-byte entries, 16-byte aligned).
+static size_t col_smem(int log_r) {
+    const size_t words = (size_t)col_vstride(log_r) * (1 << col_group_log(log_r));
+    return ((words * sizeof(u32) + 15) & ~(size_t)15) + ((size_t)8 << log_r);
+}
 
 template <class K>
 static cudaError_t opt_in(K kernel) {
@@ -256,7 +273,7 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
     auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
     if (init) return opt_in(k);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, square ? 1 : 2);
-    const size_t smem = (size_t)col_vstride(L) * (1 << col_group_log(L)) * sizeof(u32);
+    const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
@@ -276,7 +293,7 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
     auto k = k_inv_cols<A, L>;
     if (init) return opt_in(k);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np);
-    const size_t smem = (size_t)col_vstride(L) * (1 << col_group_log(L)) * sizeof(u32);
+    const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
