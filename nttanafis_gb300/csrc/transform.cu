@@ -102,7 +102,7 @@ template <class A, bool SIGNED, int LOG_R>
 __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     using M = ColumnMap<LOG_R>;
-    constexpr int B = 8;  // sweeps per batch; B*RS is a multiple of 32, so batch offsets are exact
+    constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;  // sweeps per batch; B*RS is a multiple of 32
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
     const int op = blockIdx.z;
@@ -207,7 +207,7 @@ template <class A, int LOG_R>
 __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     using M = ColumnMap<LOG_R>;
-    constexpr int B = 8;
+    constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
