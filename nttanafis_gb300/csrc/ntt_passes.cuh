@@ -100,13 +100,19 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, int nvec, int vstr
     }
 }
 
+// Levels per register block (2^RB points per thread and pass).
+#ifndef NTT_MAX_RB
+#define NTT_MAX_RB 4
+#endif
+constexpr int kMaxRB = NTT_MAX_RB;
+
 // Full forward transform of nvec vectors of 2^LOG_N points; ends with a barrier.
 template <class A, int LOG_N, int NT, int LEVEL = 0>
 __device__ __forceinline__ void dif_full(u32* s, int nvec, int vstride, const uint2* tw, u32 p) {
-    if constexpr (LOG_N - LEVEL >= 4) {
-        dif_pass<A, LOG_N, LEVEL, 4, NT>(s, nvec, vstride, tw, p);
+    if constexpr (LOG_N - LEVEL >= kMaxRB) {
+        dif_pass<A, LOG_N, LEVEL, kMaxRB, NT>(s, nvec, vstride, tw, p);
         __syncthreads();
-        dif_full<A, LOG_N, NT, LEVEL + 4>(s, nvec, vstride, tw, p);
+        dif_full<A, LOG_N, NT, LEVEL + kMaxRB>(s, nvec, vstride, tw, p);
     } else if constexpr (LOG_N - LEVEL > 0) {
         dif_pass<A, LOG_N, LEVEL, LOG_N - LEVEL, NT>(s, nvec, vstride, tw, p);
         __syncthreads();
@@ -117,15 +123,15 @@ __device__ __forceinline__ void dif_full(u32* s, int nvec, int vstride, const ui
 template <class A, int LOG_N, int NT, int LEVEL = -1>
 __device__ __forceinline__ void dit_full(u32* s, int nvec, int vstride, const uint2* tw, u32 p) {
     if constexpr (LEVEL < 0) {
-        constexpr int R0 = LOG_N & 3;
+        constexpr int R0 = LOG_N % kMaxRB;
         if constexpr (R0 > 0) {
             dit_pass<A, LOG_N, 0, R0, NT>(s, nvec, vstride, tw, p);
             __syncthreads();
         }
         dit_full<A, LOG_N, NT, R0>(s, nvec, vstride, tw, p);
     } else if constexpr (LEVEL < LOG_N) {
-        dit_pass<A, LOG_N, LEVEL, 4, NT>(s, nvec, vstride, tw, p);
+        dit_pass<A, LOG_N, LEVEL, kMaxRB, NT>(s, nvec, vstride, tw, p);
         __syncthreads();
-        dit_full<A, LOG_N, NT, LEVEL + 4>(s, nvec, vstride, tw, p);
+        dit_full<A, LOG_N, NT, LEVEL + kMaxRB>(s, nvec, vstride, tw, p);
     }
 }

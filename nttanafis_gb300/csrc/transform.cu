@@ -22,10 +22,18 @@
 namespace ntt {
 
 constexpr int kThreads = 256;
+#ifndef NTT_ROW_THREADS
+#define NTT_ROW_THREADS 256
+#endif
+#ifndef NTT_COLS_LOG_G
+#define NTT_COLS_LOG_G 3
+#endif
+// Threads of a row-pass CTA.
+constexpr int kRowThreads = NTT_ROW_THREADS;
 
 // log2 of the columns one CTA of a column pass owns: 8 columns, so a row segment
 // is one 32-byte sector of u32 residues (two of u64 limbs).
-__host__ __device__ constexpr int col_group_log(int) { return 3; }
+__host__ __device__ constexpr int col_group_log(int) { return NTT_COLS_LOG_G; }
 // Padded words per column in shared memory: congruent to 32/G mod 32 so that a
 // warp's G columns times 32/G rows fall in distinct banks.
 __host__ __device__ constexpr int col_vstride(int log_r) {
@@ -155,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
 // Row pass: forward rows of a (and b), pointwise product, inverse rows, inverse
 // four-step twiddle with the 2^32 / T scale. grid = (R, np); writes over a's rows.
 template <class A, bool SQUARE, int LOG_C>
-__global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ TransformArgs g) {
+__global__ void __launch_bounds__(kRowThreads) k_rows(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     constexpr int C = 1 << LOG_C;
     constexpr int VS = padded_len(C);
@@ -168,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ Trans
     u32* sa = sm;
     u32* sb = sm + VS;
 #pragma unroll 4
-    for (int q = threadIdx.x; q < (C >> 2); q += kThreads) {
+    for (int q = threadIdx.x; q < (C >> 2); q += kRowThreads) {
         const int k = pad_index(q << 2);
         const uint4 v = __ldcs(ra + q);
         sa[k] = v.x; sa[k + 1] = v.y; sa[k + 2] = v.z; sa[k + 3] = v.w;
@@ -178,18 +186,18 @@ __global__ void __launch_bounds__(kThreads) k_rows(const __grid_constant__ Trans
         }
     }
     __syncthreads();
-    dif_full<A, LOG_C, kThreads>(sm, SQUARE ? 1 : 2, VS, pp.fwd, pp.p);
-    for (int i = threadIdx.x; i < C; i += kThreads) {
+    dif_full<A, LOG_C, kRowThreads>(sm, SQUARE ? 1 : 2, VS, pp.fwd, pp.p);
+    for (int i = threadIdx.x; i < C; i += kRowThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
         sa[k] = A::pointwise(x, SQUARE ? x : sb[k], pp.p, pp.pni);
     }
     __syncthreads();
-    dit_full<A, LOG_C, kThreads>(sa, 1, VS, pp.inv, pp.p);
+    dit_full<A, LOG_C, kRowThreads>(sa, 1, VS, pp.inv, pp.p);
     const u32 rowexp = __brev((u32)row) >> (32 - g.log_r);
     const u32 lo_mask = (1u << g.s_bits) - 1;
 #pragma unroll 4
-    for (int q = threadIdx.x; q < (C >> 2); q += kThreads) {
+    for (int q = threadIdx.x; q < (C >> 2); q += kRowThreads) {
         const int k = pad_index(q << 2);
         u32 v[4];
 #pragma unroll
@@ -284,7 +292,7 @@ static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st,
     if (init) return opt_in(k);
     const dim3 grid(1u << g.log_r, g.np);
     const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
-    k<<<grid, kThreads, smem, st>>>(g);
+    k<<<grid, kRowThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
 
