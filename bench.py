@@ -196,6 +196,78 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def batched_section(dev, stream, count: int = 4096, reps: int = 3) -> dict:
+    """Batched configuration: `count` products (log-uniform 256..65536 limbs, ratio
+    up to 8:1, 25% squares) through the batch layer in one enqueue, against the
+    same products issued one workspace call each, on the same resident inputs."""
+    import torch
+
+    import nttanafis_gb300 as ntt
+    from nttanafis_gb300.workloads import batched_shapes
+
+    shapes = batched_shapes(count, seed=5)
+    reqs, singles = [], []
+    limbs = 0
+    for s in shapes:
+        a_h, b_h = s.operands()
+        a = torch.from_numpy(a_h.view(np.int64)).to(dev)
+        b = a if s.kind == "sqr" else torch.from_numpy(b_h.view(np.int64)).to(dev)
+        d = torch.empty(s.out_len(), dtype=torch.int64, device=dev)
+        reqs.append(ntt.Request(d, a, b))
+        singles.append((d, a, b))
+        limbs += s.la + s.lb
+    batch = ntt.GpuBatch()
+    packed = ntt.GpuBatch.pack(reqs)
+    ws = ntt.GpuMulWorkspace()
+    # warm-up (tables, arenas) of both forms
+    assert batch.run(packed, stream), ntt.last_error()
+    for d, a, b in singles[:64]:
+        assert ws.mul_device(d, a, b, stream), ntt.last_error()
+    torch.cuda.synchronize(dev)
+
+    def timed(fn) -> float:
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            best = min(best, max(e0.elapsed_time(e1) / 1000.0, time.perf_counter() - t0))
+        return best
+
+    launches0 = ntt.kernel_launches()
+    t_batch = timed(lambda: batch.run(packed, stream))
+    batch_launches = (ntt.kernel_launches() - launches0) // reps
+    # parity of a sample of members against single calls
+    sample_ok = True
+    import random
+
+    rnd = random.Random(1)
+    for i in rnd.sample(range(count), 16):
+        d, a, b = singles[i]
+        got = d.clone()
+        ref = torch.empty_like(d)
+        assert ws.mul_device(ref, a, b, stream)
+        torch.cuda.synchronize(dev)
+        sample_ok &= bool(torch.equal(got, ref))
+    launches0 = ntt.kernel_launches()
+    t_plain = timed(lambda: [ws.mul_device(d, a, b, stream) for d, a, b in singles])
+    plain_launches = (ntt.kernel_launches() - launches0) // reps
+    batch.close()
+    ws.close()
+    return {
+        "workload": f"{count} products, log-uniform 256..65536 limbs, ratio <= 8:1, 25% squares (seed 5)",
+        "products_per_s": count / t_batch, "plain_products_per_s": count / t_plain,
+        "speedup_vs_plain": t_plain / t_batch, "ms_batch": 1000 * t_batch, "ms_plain": 1000 * t_plain,
+        "launches_batch": batch_launches, "launches_plain": plain_launches, "limbs_in": limbs,
+        "parity_sample_ok": sample_ok,
+        "timing": "best of 3, max(device events, host wall) per enqueue+completion",
+    }
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -335,6 +407,8 @@ def run_gpu(args) -> None:
         "gpu_launches": launches, "wall_s": t_wall, "parity": {"fingerprint_ok": fingerprint_ok},
     }
     line["clocks"] = sampler.summary()
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_section(dev, stream)
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
         multi = cpu_sample(cores, seconds=args.cpu_seconds)
@@ -358,6 +432,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-configuration section")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.warmup < 3:

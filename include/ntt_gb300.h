@@ -135,6 +135,37 @@ uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_d
                                            size_t dst_len, const uint64_t* d_a, size_t a_len,
                                            const uint64_t* d_b, size_t b_len, void* stream);
 
+/* One member of a batch (device pointers). kind 0: product a*b (a square when
+ * a == b and a_len == b_len; empty operands write zeros); kind 1: convolution under
+ * the bounds max_a, max_b, two's complement when is_signed (ConvPlan rules). dst
+ * must hold dst_len >= the result's limbs. */
+typedef struct ntt_request {
+    uint64_t* dst;
+    uint64_t dst_len;
+    const uint64_t* a;
+    const uint64_t* b;
+    uint64_t a_len;
+    uint64_t b_len;
+    uint32_t kind;
+    uint32_t is_signed;
+    uint64_t max_a;
+    uint64_t max_b;
+} ntt_request;
+
+typedef struct ntt_batch ntt_batch;
+
+/* Batch executor bound to the current device. It owns a grow-only arena for the
+ * members' residues and a descriptor buffer; calls on one batch object must be
+ * ordered on one stream (use one object per concurrent stream). No counterpart in
+ * the reference crate: it is the batched layer over MulPlan::mul / ConvPlan::convolve. */
+ntt_batch* ntt_batch_new(void);
+void ntt_batch_free(ntt_batch* batch);
+/* Enqueues every request on `stream`: members are grouped by transform class and
+ * each class runs as one launch per kernel. Returns 0 and launches nothing when a
+ * request has no plan or a short dst (message in ntt_last_error()). */
+uint8_t ntt_batch_run_device(ntt_batch* batch, const ntt_request* requests, size_t count,
+                             void* stream);
+
 /* Largest product (a_len + b_len - 1 coefficients) of ntt_mul_noalloc_device, and
  * the device memory its static arrays hold on every GPU that loads the library. */
 #define NTT_NOALLOC_MAX_COEFFICIENTS 4096

@@ -5,7 +5,9 @@ ConvPlan/ConvWorkspace."""
 from .api import (  # noqa: F401
     ConvPlan,
     GpuConvWorkspace,
+    GpuBatch,
     GpuMulWorkspace,
+    Request,
     MulPlan,
     exported_symbols,
     kernel_launches,

@@ -91,6 +91,9 @@ _SIGNATURES = [
     ("ntt_conv_workspace_convolve_device", ctypes.c_uint8,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_batch_new", ctypes.c_void_p, []),
+    ("ntt_batch_free", None, [ctypes.c_void_p]),
+    ("ntt_batch_run_device", ctypes.c_uint8, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("ntt_mul_noalloc_device", ctypes.c_uint8,
      [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p]),
@@ -332,3 +335,75 @@ class GpuConvWorkspace:
         pb, nb = _dev(b)
         return bool(self._lib.ntt_conv_workspace_convolve_device(self._ws, d, nd, pa, na, pb, nb,
                                                                  _stream_handle(stream)))
+
+
+class NttRequest(ctypes.Structure):
+    _fields_ = [
+        ("dst", ctypes.c_void_p),
+        ("dst_len", ctypes.c_uint64),
+        ("a", ctypes.c_void_p),
+        ("b", ctypes.c_void_p),
+        ("a_len", ctypes.c_uint64),
+        ("b_len", ctypes.c_uint64),
+        ("kind", ctypes.c_uint32),
+        ("is_signed", ctypes.c_uint32),
+        ("max_a", ctypes.c_uint64),
+        ("max_b", ctypes.c_uint64),
+    ]
+
+
+@dataclass
+class Request:
+    """One batch member on device tensors: a product (kind "mul"; the same tensor
+    twice squares it) or a convolution (kind "conv") under ConvPlan's bounds."""
+
+    dst: object
+    a: object
+    b: object
+    kind: str = "mul"
+    max_a: int = 0
+    max_b: int = 0
+    signed: bool = False
+
+    def raw(self) -> NttRequest:
+        d, nd = _dev(self.dst)
+        pa, na = _dev(self.a)
+        pb, nb = _dev(self.b)
+        return NttRequest(d, nd, pa, pb, na, nb, 0 if self.kind == "mul" else 1, int(self.signed), self.max_a,
+                          self.max_b)
+
+
+class GpuBatch:
+    """Batched executor: many exact products/convolutions per enqueue, grouped by
+    transform class (one launch per kernel and class). Calls on one object must be
+    ordered on one stream."""
+
+    def __init__(self) -> None:
+        self._lib = library()
+        self._b = self._lib.ntt_batch_new()
+        if not self._b:
+            raise RuntimeError(f"cannot create a batch: {last_error()}")
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            self._lib.ntt_batch_free(self._b)
+            self._b = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def pack(requests) -> ctypes.Array:
+        arr = (NttRequest * len(requests))()
+        for i, r in enumerate(requests):
+            arr[i] = r.raw() if isinstance(r, Request) else r
+        return arr
+
+    def run(self, requests, stream=None) -> bool:
+        """Enqueues `requests` (Request objects or a packed array) on `stream`."""
+        arr = requests if isinstance(requests, ctypes.Array) else self.pack(requests)
+        return bool(self._lib.ntt_batch_run_device(self._b, ctypes.cast(arr, ctypes.c_void_p), len(arr),
+                                                   _stream_handle(stream)))

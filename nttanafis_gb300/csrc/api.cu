@@ -824,6 +824,195 @@ int ntt_timing_stop(float* ms, int capacity) {
     return out;
 }
 
+// ---------------------------------------------------------------------------------
+// Batches: many products and convolutions in one enqueue. Members are grouped by
+// transform class (kind, length, primes, sign); each class runs as one launch of
+// every kernel of its path, with the member index in the last grid dimension.
+
+struct ntt_batch {
+    int device = 0;
+    DeviceBuf arena;  // residues and carry flags of every member
+    DeviceBuf desc;   // member descriptors
+    ProductDesc* host_desc = nullptr;
+    size_t host_cap = 0;
+    cudaEvent_t staged = nullptr;  // the last descriptor upload has been read
+    bool pending = false;
+};
+
+ntt_batch* ntt_batch_new(void) {
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return nullptr;
+    ntt_batch* b = new ntt_batch();
+    b->device = dev;
+    if (!cuda_ok(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate")) {
+        delete b;
+        return nullptr;
+    }
+    return b;
+}
+
+void ntt_batch_free(ntt_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->pending) cudaEventSynchronize(b->staged);
+    cudaDeviceSynchronize();
+    b->arena.release();
+    b->desc.release();
+    if (b->host_desc) cudaFreeHost(b->host_desc);
+    cudaEventDestroy(b->staged);
+    delete b;
+}
+
+namespace {
+struct Member {
+    size_t index;
+    Geom g;
+    bool square;
+    u64 offset;  // bytes into the arena
+};
+}  // namespace
+
+uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count, void* stream) {
+    if (!b || (!reqs && count)) return fail("null argument");
+    if (!cuda_ok(cudaSetDevice(b->device), "cudaSetDevice")) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    // Plan every member first: a batch with an inadmissible member launches nothing.
+    std::vector<Member> members;
+    members.reserve(count);
+    std::vector<size_t> empties;
+    u64 arena_bytes = 0;
+    for (size_t i = 0; i < count; ++i) {
+        const ntt_request& r = reqs[i];
+        Member m;
+        m.index = i;
+        if (r.kind == 0) {
+            if (r.a_len == 0 || r.b_len == 0) {
+                if ((u64)r.a_len + r.b_len > r.dst_len) return fail("destination is shorter than the product");
+                empties.push_back(i);
+                continue;
+            }
+            if (!plan_mul(r.a_len, r.b_len, m.g)) return 0;
+        } else if (r.kind == 1) {
+            if (!plan_conv(r.a_len, r.b_len, r.max_a, r.max_b, (int)r.is_signed, m.g)) return 0;
+        } else {
+            return fail("unknown request kind");
+        }
+        if (r.dst_len < m.g.out_len) return fail("destination is shorter than the result");
+        m.square = r.a == r.b && r.a_len == r.b_len;
+        m.offset = arena_bytes;
+        arena_bytes += (m.g.scratch_bytes(m.square) + 255) & ~(u64)255;
+        members.push_back(m);
+    }
+    for (size_t i : empties)
+        if (!cuda_ok(cudaMemsetAsync(reqs[i].dst, 0, ((size_t)reqs[i].a_len + reqs[i].b_len) * 8, st), "zero product"))
+            return 0;
+    if (members.empty()) return 1;
+    // Group by class: kind, schoolbook, transform length, primes, sign.
+    std::sort(members.begin(), members.end(), [](const Member& x, const Member& y) {
+        return std::make_tuple(x.g.conv, x.g.schoolbook, x.g.log_t, x.g.np, x.g.sign, x.index) <
+               std::make_tuple(y.g.conv, y.g.schoolbook, y.g.log_t, y.g.np, y.g.sign, y.index);
+    });
+    if (!b->arena.ensure(std::max<u64>(arena_bytes, 256)) || !b->desc.ensure(members.size() * sizeof(ProductDesc)))
+        return 0;
+    if (b->pending && !cuda_ok(cudaEventSynchronize(b->staged), "descriptor staging")) return 0;
+    b->pending = false;
+    if (b->host_cap < members.size()) {
+        if (b->host_desc) cudaFreeHost(b->host_desc);
+        b->host_desc = nullptr;
+        b->host_cap = 0;
+        if (!cuda_ok(cudaHostAlloc((void**)&b->host_desc, members.size() * sizeof(ProductDesc), cudaHostAllocDefault),
+                     "cudaHostAlloc"))
+            return 0;
+        b->host_cap = members.size();
+    }
+    uint8_t* arena = (uint8_t*)b->arena.ptr;
+    for (size_t k = 0; k < members.size(); ++k) {
+        const Member& m = members[k];
+        const ntt_request& r = reqs[m.index];
+        ProductDesc& d = b->host_desc[k];
+        d.a = r.a;
+        d.b = m.square ? r.a : r.b;
+        d.la = r.a_len;
+        d.lb = m.square ? r.a_len : r.b_len;
+        d.spec = (u32*)(arena + m.offset);
+        d.conv_len = m.g.conv_len;
+        d.dst = r.dst;
+        d.out_len = m.g.out_len;
+        d.agg = arena + m.offset + ((m.g.spec_words(m.square) * 4 + 255) & ~(u64)255);
+        d.square = m.square ? 1u : 0u;
+        d.stride = (u32)m.g.stride;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(b->desc.ptr, b->host_desc, members.size() * sizeof(ProductDesc),
+                                 cudaMemcpyHostToDevice, st),
+                 "descriptor upload") ||
+        !cuda_ok(cudaEventRecord(b->staged, st), "cudaEventRecord"))
+        return 0;
+    b->pending = true;
+    const ProductDesc* dev_desc = (const ProductDesc*)b->desc.ptr;
+    constexpr size_t kMaxLaunchMembers = 16384;  // 2 * members fits gridDim.z
+    size_t k = 0;
+    while (k < members.size()) {
+        const Geom& g0 = members[k].g;
+        size_t end = k + 1;
+        while (end < members.size() && end - k < kMaxLaunchMembers && members[end].g.conv == g0.conv &&
+               members[end].g.schoolbook == g0.schoolbook && members[end].g.log_t == g0.log_t &&
+               members[end].g.np == g0.np && members[end].g.sign == g0.sign)
+            ++end;
+        const int n = (int)(end - k);
+        if (g0.conv && g0.schoolbook) {
+            for (size_t i = k; i < end; ++i) {
+                const ProductDesc& d = b->host_desc[i];
+                g_launches += 1;
+                if (!cuda_ok(launch_conv_schoolbook(d.a, d.la, d.b, d.lb, d.dst, (int)d.stride, g0.sign != 0, st),
+                             "conv schoolbook launch"))
+                    return 0;
+            }
+            k = end;
+            continue;
+        }
+        TransformArgs ta;
+        memset(&ta, 0, sizeof(ta));
+        CrtParams cp;
+        if (!prepare_params(g0, ta.ps, cp)) return 0;
+        ta.batch = dev_desc + k;
+        ta.count = n;
+        ta.np = g0.np;
+        ta.log_t = g0.log_t;
+        ta.wide = g0.wide;
+        const bool sign = g0.sign != 0;
+        if (g0.log_t <= kMaxBlockLog) {
+            g_launches += 1;
+            if (!cuda_ok(launch_small(ta, false, sign, st), "batched transform launch")) return 0;
+        } else {
+            ta.log_r = g0.log_t / 2;
+            ta.log_c = g0.log_t - ta.log_r;
+            ta.s_bits = s_bits_of(g0.log_t);
+            g_launches += 3;
+            if (!cuda_ok(launch_fwd_cols(ta, false, sign, st), "batched column pass launch") ||
+                !cuda_ok(launch_rows(ta, false, st), "batched row pass launch") ||
+                !cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch"))
+                return 0;
+        }
+        if (g0.conv) {
+            u64 max_conv = 0;
+            for (size_t i = k; i < end; ++i) max_conv = std::max(max_conv, members[i].g.conv_len);
+            g_launches += 1;
+            if (!cuda_ok(launch_crt_conv_batch(dev_desc + k, n, max_conv, g0.log_t, cp, st), "batched CRT launch"))
+                return 0;
+        } else {
+            u64 max_out = 0;
+            for (size_t i = k; i < end; ++i) max_out = std::max(max_out, members[i].g.out_len);
+            g_launches += 2;
+            if (!cuda_ok(launch_crt_mul_batch(dev_desc + k, n, (int)((max_out + kCrtTile - 1) / kCrtTile), g0.log_t,
+                                              cp, st),
+                         "batched CRT launch"))
+                return 0;
+        }
+        k = end;
+    }
+    return 1;
+}
+
 const char* ntt_last_error(void) { return g_error.c_str(); }
 uint64_t ntt_kernel_launches(void) { return g_launches.load(); }
 const char* ntt_version(void) { return "nttanafis_gb300 0.1.0 (sm_103a)"; }

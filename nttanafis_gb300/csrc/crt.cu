@@ -143,7 +143,17 @@ template <int NP>
 __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__ resid, int log_t,
                                                           u64 conv_len, u64 out_len, u64* __restrict__ dst,
                                                           uint8_t* __restrict__ agg,
-                                                          const __grid_constant__ CrtParams cp) {
+                                                          const __grid_constant__ CrtParams cp,
+                                                          const ProductDesc* __restrict__ batch) {
+    if (batch) {  // member blockIdx.y of a batch: grid.x covers its largest member
+        const ProductDesc& d = batch[blockIdx.y];
+        resid = d.spec;
+        conv_len = d.conv_len;
+        out_len = d.out_len;
+        dst = d.dst;
+        agg = d.agg;
+        if ((u64)blockIdx.x * kCrtTile >= out_len) return;
+    }
     constexpr int kBack = 4;  // coefficients before the tile that reach into it (l64 <= 4)
     constexpr int kWords = kCrtTile + kBack;
     constexpr int kChunks = kCrtTile / (32 * (kCrtThreads / 32));  // 4 chunks of 32 limbs per warp
@@ -231,7 +241,16 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
 // limb that is not all ones; the all-ones limbs below it become zero. Warps take
 // such tiles in turn; random operands almost never produce one.
 __global__ void __launch_bounds__(1024) k_carry(const uint8_t* __restrict__ agg, uint8_t* __restrict__ cin,
-                                                int tiles, u64* __restrict__ dst, u64 out_len) {
+                                                int tiles, u64* __restrict__ dst, u64 out_len,
+                                                const ProductDesc* __restrict__ batch) {
+    if (batch) {  // one CTA per member
+        const ProductDesc& d = batch[blockIdx.x];
+        out_len = d.out_len;
+        tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
+        agg = d.agg;
+        cin = d.agg + tiles;
+        dst = d.dst;
+    }
     constexpr int kList = 1024;
     __shared__ int s_count;
     __shared__ int s_list[kList];
@@ -288,14 +307,27 @@ __global__ void __launch_bounds__(1024) k_carry(const uint8_t* __restrict__ agg,
 template <int NP>
 __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict__ resid, int log_t,
                                                            u64 conv_len, u64* __restrict__ dst,
-                                                           const __grid_constant__ CrtParams cp) {
+                                                           const __grid_constant__ CrtParams cp,
+                                                           const ProductDesc* __restrict__ batch) {
+    int stride = cp.stride;
+    if (batch) {  // member blockIdx.y of a batch
+        const ProductDesc& d = batch[blockIdx.y];
+        resid = d.spec;
+        conv_len = d.conv_len;
+        dst = d.dst;
+        stride = (int)d.stride;
+    }
     const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= conv_len) return;
     u64 w[4];
     crt_coeff<NP>(resid, log_t, k, cp, w);
     const u64 fill = (w[3] >> 63) ? ~0ull : 0ull;
-    u64* out = dst + k * (u64)cp.stride;
-    for (int s = 0; s < cp.stride; ++s) out[s] = s < 4 ? w[s] : fill;
+    u64* out = dst + k * (u64)stride;
+    out[0] = w[0];
+    if (stride > 1) out[1] = w[1];
+    if (stride > 2) out[2] = w[2];
+    if (stride > 3) out[3] = w[3];
+    for (int s = 4; s < stride; ++s) out[s] = fill;
 }
 
 // Short operand (<= 24 terms): exact sums of 128-bit products in three limbs.
@@ -332,10 +364,51 @@ template <int NP>
 static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
                        const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
     const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
-    k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst, agg, cp);
+    k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst, agg, cp, nullptr);
     if (mark) mark(st);
-    k_carry<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles, dst, out_len);
+    k_carry<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles, dst, out_len, nullptr);
     if (mark) mark(st);
+}
+
+template <int NP>
+static void crt_mul_batch_np(const ProductDesc* batch, int count, int max_tiles, int log_t, const CrtParams& cp,
+                             cudaStream_t st) {
+    k_crt_mul<NP><<<dim3(max_tiles, count), kCrtThreads, 0, st>>>(nullptr, log_t, 0, 0, nullptr, nullptr, cp,
+                                                                   batch);
+    k_carry<<<count, 1024, 0, st>>>(nullptr, nullptr, 0, nullptr, 0, batch);
+}
+
+cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_tiles, int log_t,
+                                 const CrtParams& cp, cudaStream_t st) {
+    switch (cp.np) {
+        case 1: crt_mul_batch_np<1>(batch, count, max_tiles, log_t, cp, st); break;
+        case 2: crt_mul_batch_np<2>(batch, count, max_tiles, log_t, cp, st); break;
+        case 3: crt_mul_batch_np<3>(batch, count, max_tiles, log_t, cp, st); break;
+        case 4: crt_mul_batch_np<4>(batch, count, max_tiles, log_t, cp, st); break;
+        case 5: crt_mul_batch_np<5>(batch, count, max_tiles, log_t, cp, st); break;
+        case 6: crt_mul_batch_np<6>(batch, count, max_tiles, log_t, cp, st); break;
+        case 7: crt_mul_batch_np<7>(batch, count, max_tiles, log_t, cp, st); break;
+        case 8: crt_mul_batch_np<8>(batch, count, max_tiles, log_t, cp, st); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
+                                  const CrtParams& cp, cudaStream_t st) {
+    const dim3 grid((unsigned)((max_conv_len + kCrtThreads - 1) / kCrtThreads), count);
+    switch (cp.np) {
+        case 1: k_crt_conv<1><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 2: k_crt_conv<2><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 3: k_crt_conv<3><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 4: k_crt_conv<4><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 5: k_crt_conv<5><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 6: k_crt_conv<6><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 7: k_crt_conv<7><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        case 8: k_crt_conv<8><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
@@ -359,14 +432,14 @@ cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst,
     (void)sign;  // the quotient bias in cp selects signed rounding
     const unsigned blocks = (unsigned)((conv_len + kCrtThreads - 1) / kCrtThreads);
     switch (cp.np) {
-        case 1: k_crt_conv<1><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 2: k_crt_conv<2><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 3: k_crt_conv<3><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 4: k_crt_conv<4><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 5: k_crt_conv<5><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 6: k_crt_conv<6><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 7: k_crt_conv<7><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
-        case 8: k_crt_conv<8><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp); break;
+        case 1: k_crt_conv<1><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 2: k_crt_conv<2><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 3: k_crt_conv<3><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 4: k_crt_conv<4><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 5: k_crt_conv<5><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 6: k_crt_conv<6><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 7: k_crt_conv<7><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
+        case 8: k_crt_conv<8><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

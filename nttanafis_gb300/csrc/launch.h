@@ -17,8 +17,28 @@ constexpr int kMaxLogT = 25;
 // Output limbs per CTA of the CRT + carry kernel.
 constexpr int kCrtTile = 1024;
 
-// Operands and geometry of one transform-domain product.
+// One product or convolution of a batch, read by the kernels from device memory.
+// All members of one launch share the transform length, the primes and the sign
+// mode; everything else varies per member.
+struct ProductDesc {
+    const u64* a;
+    const u64* b;      // == a for a square
+    u64 la, lb;
+    u32* spec;         // this member's residues ([2][np][T] u32)
+    u64 conv_len;
+    u64* dst;
+    u64 out_len;       // limbs of a product
+    uint8_t* agg;      // carry flags of a product (2 bytes per output tile)
+    u32 square;
+    u32 stride;        // convolution limbs per coefficient
+};
+
+// Operands and geometry of one transform-domain product. With `batch` set, the
+// kernels run `count` members: the member index is the launch's last grid
+// dimension and the member fields override a, b, la, lb, spec and conv_len.
 struct TransformArgs {
+    const ProductDesc* batch;
+    int count;
     const u64* a;
     const u64* b;
     u64 la, lb;
@@ -58,6 +78,12 @@ cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_le
                            void (*mark)(cudaStream_t) = nullptr);
 cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst, bool sign,
                             const CrtParams& cp, cudaStream_t st);
+// Batched forms: every member of `batch` (device array of `count` descriptors)
+// shares log_t and the prime set of `cp`.
+cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_tiles, int log_t,
+                                 const CrtParams& cp, cudaStream_t st);
+cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
+                                  const CrtParams& cp, cudaStream_t st);
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
                                    int stride, bool sign, cudaStream_t st);
 // Scratch bytes the CRT carry pass needs for `out_len` output limbs.

@@ -23,7 +23,7 @@ namespace ntt {
 
 constexpr int kThreads = 256;
 #ifndef NTT_ROW_THREADS
-#define NTT_ROW_THREADS 256
+#define NTT_ROW_THREADS 128
 #endif
 #ifndef NTT_COLS_LOG_G
 #define NTT_COLS_LOG_G 3
@@ -46,31 +46,51 @@ __device__ __forceinline__ u32 reduce_coefficient(u64 x, const PrimeParams& pp) 
     return SIGNED ? reduce_signed<A>(x, pp) : reduce_limb<A>(x, pp);
 }
 
+// Operands of the launch member a CTA works on (TransformArgs::batch).
+struct Member {
+    const u64* a;
+    const u64* b;
+    u64 la, lb;
+    u32* spec;
+    u64 conv_len;
+    bool square;
+};
+
+__device__ __forceinline__ Member member_of(const TransformArgs& g, int idx, bool square) {
+    if (g.batch) {
+        const ProductDesc& d = g.batch[idx];
+        return Member{d.a, d.b, d.la, d.lb, d.spec, d.conv_len, d.square != 0};
+    }
+    return Member{g.a, g.b, g.la, g.lb, g.spec, g.conv_len, square};
+}
+
 // One CTA transforms one prime: pack, forward a (and b), pointwise, inverse, scale.
+// grid = (np, members).
 template <class A, bool SQUARE, bool SIGNED, int LOG_N>
 __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     constexpr int N = 1 << LOG_N;
     constexpr int VS = padded_len(N);
     const PrimeParams& pp = g.ps.pr[blockIdx.x];
+    const Member m = member_of(g, blockIdx.y, SQUARE);
     u32* sa = sm;
     u32* sb = sm + VS;
     for (int i = threadIdx.x; i < N; i += kThreads) {
-        sa[pad_index(i)] = (u64)i < g.la ? reduce_coefficient<A, SIGNED>(__ldg(g.a + i), pp) : 0u;
-        if (!SQUARE) sb[pad_index(i)] = (u64)i < g.lb ? reduce_coefficient<A, SIGNED>(__ldg(g.b + i), pp) : 0u;
+        sa[pad_index(i)] = (u64)i < m.la ? reduce_coefficient<A, SIGNED>(__ldg(m.a + i), pp) : 0u;
+        if (!m.square) sb[pad_index(i)] = (u64)i < m.lb ? reduce_coefficient<A, SIGNED>(__ldg(m.b + i), pp) : 0u;
     }
     __syncthreads();
-    dif_full<A, LOG_N, kThreads>(sm, SQUARE ? 1 : 2, VS, pp.fwd, pp.p);
+    dif_full<A, LOG_N, kThreads>(sm, m.square ? 1 : 2, VS, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < N; i += kThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
-        const u32 y = SQUARE ? x : sb[k];
+        const u32 y = m.square ? x : sb[k];
         sa[k] = A::mulc(A::pointwise(x, y, pp.p, pp.pni), pp.scale, pp.p);
     }
     __syncthreads();
     dit_full<A, LOG_N, kThreads>(sa, 1, VS, pp.inv, pp.p);
-    u32* out = g.spec + ((size_t)blockIdx.x << LOG_N);
-    for (int i = threadIdx.x; i < (int)g.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
+    u32* out = m.spec + ((size_t)blockIdx.x << LOG_N);
+    for (int i = threadIdx.x; i < (int)m.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
 }
 
 // Copies the level-major root table of a 2^LOG_N-point transform (entries below
@@ -113,10 +133,13 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
     constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;  // sweeps per batch; B*RS is a multiple of 32
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
-    const int op = blockIdx.z;
+    // grid.z: operands (1 or 2) of one member, or 2 per member in a batch
+    const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z;
+    const Member m = member_of(g, g.batch ? (blockIdx.z >> 1) : 0, false);
+    if (op && m.square) return;
     const PrimeParams& pp = g.ps.pr[prime];
-    const u64* __restrict__ src = op ? g.b : g.a;
-    const u64 len = op ? g.lb : g.la;
+    const u64* __restrict__ src = op ? m.b : m.a;
+    const u64 len = op ? m.lb : m.la;
     const int log_c = g.log_c;
     const u32 col = (u32)(blockIdx.x << M::LOG_G) + M::col();
     const int r0 = M::row0();
@@ -141,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
     __syncthreads();
     dif_full<A, LOG_R, kThreads>(sm, M::G, M::VS, tw, pp.p);
     // Four-step twiddle w_T^(col * k1) with k1 = bitrev(row), then the store.
-    u32* dst = g.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
+    u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
     const u32 lo_mask = (1u << g.s_bits) - 1;
     const u32 e0 = col * (__brev((u32)r0) >> (32 - LOG_R));
 #pragma unroll 1
@@ -170,9 +193,10 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(const __grid_constant__ Tr
     const int prime = blockIdx.y;
     const int row = blockIdx.x;
     const PrimeParams& pp = g.ps.pr[prime];
-    uint4* ra = reinterpret_cast<uint4*>(g.spec + ((size_t)prime << g.log_t) + ((size_t)row << LOG_C));
+    const Member m = member_of(g, blockIdx.z, SQUARE);
+    uint4* ra = reinterpret_cast<uint4*>(m.spec + ((size_t)prime << g.log_t) + ((size_t)row << LOG_C));
     const uint4* rb = reinterpret_cast<const uint4*>(
-        g.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C));
+        m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C));
     u32* sa = sm;
     u32* sb = sm + VS;
 #pragma unroll 4
@@ -180,17 +204,17 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(const __grid_constant__ Tr
         const int k = pad_index(q << 2);
         const uint4 v = __ldcs(ra + q);
         sa[k] = v.x; sa[k + 1] = v.y; sa[k + 2] = v.z; sa[k + 3] = v.w;
-        if (!SQUARE) {
+        if (!m.square) {
             const uint4 w = __ldcs(rb + q);
             sb[k] = w.x; sb[k + 1] = w.y; sb[k + 2] = w.z; sb[k + 3] = w.w;
         }
     }
     __syncthreads();
-    dif_full<A, LOG_C, kRowThreads>(sm, SQUARE ? 1 : 2, VS, pp.fwd, pp.p);
+    dif_full<A, LOG_C, kRowThreads>(sm, m.square ? 1 : 2, VS, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < C; i += kRowThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
-        sa[k] = A::pointwise(x, SQUARE ? x : sb[k], pp.p, pp.pni);
+        sa[k] = A::pointwise(x, m.square ? x : sb[k], pp.p, pp.pni);
     }
     __syncthreads();
     dit_full<A, LOG_C, kRowThreads>(sa, 1, VS, pp.inv, pp.p);
@@ -219,8 +243,9 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ T
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
+    const Member m = member_of(g, blockIdx.z, false);
     const u64 step = (u64)M::RS << g.log_c;
-    u32* const base = g.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
+    u32* const base = m.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
                       (blockIdx.x << M::LOG_G) + M::col();
     u32* s = sm + M::slot0();
     uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
@@ -272,7 +297,7 @@ static cudaError_t small_at(const TransformArgs& g, bool square, bool sign, cuda
                     : (sign ? k_small<A, false, true, L> : k_small<A, false, false, L>);
     if (init) return opt_in(k);
     const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
-    k<<<g.np, kThreads, smem, st>>>(g);
+    k<<<dim3(g.np, g.batch ? g.count : 1), kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
 
@@ -280,7 +305,7 @@ template <class A, int L>
 static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
     if (init) return opt_in(k);
-    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, square ? 1 : 2);
+    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : (square ? 1 : 2));
     const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
@@ -290,7 +315,7 @@ template <class A, int L>
 static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
     auto k = square ? k_rows<A, true, L> : k_rows<A, false, L>;
     if (init) return opt_in(k);
-    const dim3 grid(1u << g.log_r, g.np);
+    const dim3 grid(1u << g.log_r, g.np, g.batch ? g.count : 1);
     const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
     k<<<grid, kRowThreads, smem, st>>>(g);
     return cudaGetLastError();
@@ -300,7 +325,7 @@ template <class A, int L>
 static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool init) {
     auto k = k_inv_cols<A, L>;
     if (init) return opt_in(k);
-    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np);
+    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? g.count : 1);
     const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
