@@ -268,6 +268,61 @@ def batched_section(dev, stream, count: int = 4096, reps: int = 3) -> dict:
     }
 
 
+def served_section(dev, count: int = 400, rates=(2000.0, 20000.0), budget_gb: float = 8.0, slots: int = 4) -> dict:
+    """Served configuration: Poisson arrivals of products/squares (log-uniform
+    192..4,194,304 limbs) and 16/32-bit unsigned and 32-bit signed convolutions
+    (1,024..4,194,304 coefficients), continuous batching under an HBM budget, at a
+    few arrival rates; against the same requests issued one call at a time."""
+    import torch
+
+    import nttanafis_gb300 as ntt
+    from nttanafis_gb300.serve import GpuExecutor, serve
+    from nttanafis_gb300.workloads import served_stream
+
+    ex = GpuExecutor(slots, dev)
+    out = {"workload": f"{count} requests per rate; mul/sqr 192..4194304 limbs, conv 1024..4194304 coefficients "
+                       "(16-bit, 32-bit unsigned, 32-bit signed)", "budget_bytes": int(budget_gb * 2**30),
+           "slots": slots, "rates": []}
+    warm = served_stream(32, 1e9, seed=99, max_limbs=1 << 16)
+    serve(warm, ex, int(budget_gb * 2**30), slots)
+    torch.cuda.synchronize(dev)
+    for rate in rates:
+        stream = served_stream(count, rate, seed=7)
+        stats = serve(stream, ex, int(budget_gb * 2**30), slots)
+        torch.cuda.synchronize(dev)
+        finished = stats.pop("finished")
+        stats.pop("order")
+        # parity: a sample of results equals the same request computed alone
+        ok = True
+        for p in finished[:: max(1, len(finished) // 12)]:
+            ok &= bool(torch.equal(p.payload.dst, ex.alone(stream[p.rid])))
+        stats["rate_hz"] = rate
+        stats["parity_sample_ok"] = ok
+        out["rates"].append(stats)
+    # plain: the same requests one call at a time on one stream
+    stream = served_stream(count, rates[-1], seed=7)
+    payloads = [ex.prepare(item) for item in stream]
+    ws, cws = ntt.GpuMulWorkspace(), ntt.GpuConvWorkspace()
+    st = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for item, r in zip(stream, payloads):
+        if item.kind == "conv":
+            cws.prepare(ntt.ConvPlan.new(item.la, item.lb, item.max_a, item.max_a, item.signed))
+            cws.convolve_device(r.dst, r.a, r.b, st)
+        else:
+            ws.mul_device(r.dst, r.a, r.b, st)
+    torch.cuda.synchronize(dev)
+    plain = time.perf_counter() - t0
+    out["plain_requests_per_s"] = count / plain
+    best = max(r["requests_per_s"] for r in out["rates"])
+    out["speedup_vs_plain"] = best / out["plain_requests_per_s"]
+    ws.close()
+    cws.close()
+    ex.close()
+    return out
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -409,6 +464,8 @@ def run_gpu(args) -> None:
     line["clocks"] = sampler.summary()
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_section(dev, stream)
+    if rank == 0 and not args.no_served:
+        line["served"] = served_section(dev)
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
         multi = cpu_sample(cores, seconds=args.cpu_seconds)
@@ -433,6 +490,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-configuration section")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-configuration section")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.warmup < 3:
