@@ -286,9 +286,21 @@ static size_t col_smem(int log_r) {
     return ((words * sizeof(u32) + 15) & ~(size_t)15) + ((size_t)8 << log_r);
 }
 
+// Preferred shared-memory carveout (percent of the unified L1/shared capacity) of
+// the row and column passes; -1 leaves the driver's choice.
+#ifndef NTT_ROWS_CARVEOUT
+#define NTT_ROWS_CARVEOUT -1
+#endif
+#ifndef NTT_COLS_CARVEOUT
+#define NTT_COLS_CARVEOUT -1
+#endif
+
 template <class K>
-static cudaError_t opt_in(K kernel) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn);
+static cudaError_t opt_in(K kernel, int carveout = -1) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn);
+    if (e == cudaSuccess && carveout >= 0)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    return e;
 }
 
 template <class A, int L>
@@ -304,7 +316,7 @@ static cudaError_t small_at(const TransformArgs& g, bool square, bool sign, cuda
 template <class A, int L>
 static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
-    if (init) return opt_in(k);
+    if (init) return opt_in(k, NTT_COLS_CARVEOUT);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : (square ? 1 : 2));
     const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
@@ -314,7 +326,7 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
 template <class A, int L>
 static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
     auto k = square ? k_rows<A, true, L> : k_rows<A, false, L>;
-    if (init) return opt_in(k);
+    if (init) return opt_in(k, NTT_ROWS_CARVEOUT);
     const dim3 grid(1u << g.log_r, g.np, g.batch ? g.count : 1);
     const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
     k<<<grid, kRowThreads, smem, st>>>(g);
@@ -324,7 +336,7 @@ static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st,
 template <class A, int L>
 static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool init) {
     auto k = k_inv_cols<A, L>;
-    if (init) return opt_in(k);
+    if (init) return opt_in(k, NTT_COLS_CARVEOUT);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? g.count : 1);
     const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
