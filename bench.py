@@ -196,6 +196,50 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def configs_section(dev, stream, peak_gbs: float) -> list:
+    """Device time per product of every plain configuration (inputs resident), with
+    its algorithmic bytes and roofline fraction. Squares pass the same tensor twice."""
+    import torch
+
+    import oracle
+    import nttanafis_gb300 as ntt
+    from nttanafis_gb300.operands import operand, sparse_operand
+
+    ones = lambda n, s: np.full(n, np.uint64(0xFFFFFFFFFFFFFFFF), dtype=np.uint64)  # noqa: E731
+    cases = [
+        ("mul 1024x1024", 1024, 1024, operand, 8000), ("sqr 1024", 1024, 0, operand, 8000),
+        ("mul 1048576x1048576", 1 << 20, 1 << 20, operand, 100), ("sqr 1048576", 1 << 20, 0, operand, 100),
+        ("mul 1048576x131072", 1 << 20, 131072, operand, 100),
+        ("mul 1048576^2 all-ones", 1 << 20, 1 << 20, ones, 50),
+        ("mul 1048576^2 99% zero limbs", 1 << 20, 1 << 20, lambda n, s: sparse_operand(n, s, s + 1), 50),
+        ("mul 16777216x16777216", 1 << 24, 1 << 24, operand, 6), ("sqr 16777216", 1 << 24, 0, operand, 6),
+    ]
+    ws = ntt.GpuMulWorkspace()
+    out = []
+    for name, la, lb, gen, reps in cases:
+        a = torch.from_numpy(gen(la, 1).view(np.int64)).to(dev)
+        b = a if lb == 0 else torch.from_numpy(gen(lb, 2).view(np.int64)).to(dev)
+        n_out = la + (la if lb == 0 else lb)
+        d = torch.empty(n_out, dtype=torch.int64, device=dev)
+        for _ in range(3):
+            assert ws.mul_device(d, a, b, stream), ntt.last_error()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            ws.mul_device(d, a, b, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        model = oracle.model_bytes("sqr" if lb == 0 else "mul", la, lb or la)
+        out.append({"config": name, "ms_per_product": round(ms, 5), "products_per_s": round(1000.0 / ms, 1),
+                    "algorithmic_bytes": model, "roofline_frac": round(model / (ms / 1000.0) / 1e9 / peak_gbs, 4)})
+        del a, b, d
+    ws.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def batched_section(dev, stream, count: int = 4096, reps: int = 3) -> dict:
     """Batched configuration: `count` products (log-uniform 256..65536 limbs, ratio
     up to 8:1, 25% squares) through the batch layer in one enqueue, against the
@@ -462,6 +506,8 @@ def run_gpu(args) -> None:
         "gpu_launches": launches, "wall_s": t_wall, "parity": {"fingerprint_ok": fingerprint_ok},
     }
     line["clocks"] = sampler.summary()
+    if rank == 0 and not args.no_configs:
+        line["configs"] = configs_section(dev, stream, peak)
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_section(dev, stream)
     if rank == 0 and not args.no_served:
@@ -491,6 +537,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-configuration section")
     ap.add_argument("--no-served", action="store_true", help="skip the served-configuration section")
+    ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration timings")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -412,8 +412,11 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
 // ---------------------------------------------------------------------------------
 // Execution on device pointers
 
+// Enqueues one product or convolution on `st`. With `b_ready` set (an event that
+// completes when operand b is in place), the column pass of a runs first and the
+// one of b waits for that event, so b's upload overlaps a's pass.
 static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst,
-                    void* scratch, cudaStream_t st) {
+                    void* scratch, cudaStream_t st, cudaEvent_t b_ready = nullptr) {
     mark(st);
     if (g.conv && g.schoolbook) {
         g_launches += 1;
@@ -438,6 +441,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
     ta.wide = g.wide;
     const bool sign = g.sign != 0;
     if (g.log_t <= kMaxBlockLog) {
+        if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         g_launches += 1;
         if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
         mark(st);
@@ -451,8 +455,19 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         vs += ((target - vs) % 32 + 32) % 32;
         ta.vstride_col = vs;
         ta.s_bits = s_bits_of(g.log_t);
+        if (b_ready && !square) {
+            g_launches += 1;
+            ta.op_count = 1;
+            if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) return false;
+            if (!cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
+            ta.op_base = 1;
+            if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) return false;
+            ta.op_base = 0;
+            ta.op_count = 0;
+        } else if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) {
+            return false;
+        }
         g_launches += 3;
-        if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) return false;
         mark(st);
         if (!cuda_ok(launch_rows(ta, square, st), "row pass launch")) return false;
         mark(st);
@@ -518,6 +533,8 @@ using namespace ntt;
 struct ntt_mul_workspace {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t upload = nullptr;    // copies operand b while a's column pass runs
+    cudaEvent_t b_ready = nullptr;
     bool has_plan = false;
     Geom plan;
     DeviceBuf a, b, out, scratch;
@@ -526,6 +543,8 @@ struct ntt_mul_workspace {
 struct ntt_conv_workspace {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t upload = nullptr;
+    cudaEvent_t b_ready = nullptr;
     bool has_plan = false;
     Geom plan;
     DeviceBuf a, b, out, scratch;
@@ -537,7 +556,11 @@ static W* workspace_new() {
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return nullptr;
     W* ws = new W();
     ws->device = dev;
-    if (!cuda_ok(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking), "cudaStreamCreate")) {
+    if (!cuda_ok(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&ws->upload, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaEventCreateWithFlags(&ws->b_ready, cudaEventDisableTiming), "cudaEventCreate")) {
+        if (ws->stream) cudaStreamDestroy(ws->stream);
+        if (ws->upload) cudaStreamDestroy(ws->upload);
         delete ws;
         return nullptr;
     }
@@ -553,26 +576,49 @@ static void workspace_free(W* ws) {
     ws->b.release();
     ws->out.release();
     ws->scratch.release();
+    cudaEventDestroy(ws->b_ready);
+    cudaStreamDestroy(ws->upload);
     cudaStreamDestroy(ws->stream);
     delete ws;
 }
 
-// Runs a host-pointer call: copy in, execute, check, copy the result prefix out.
+// Device address of page-locked host memory, or null for other memory.
+static void* mapped_host_pointer(void* p) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
+// Runs a host-pointer call. The operands are copied in (b on a second stream,
+// overlapping a's column pass); the result is written straight into dst when dst
+// is page-locked host memory the GPU can address, and copied out otherwise. One
+// synchronisation at the end: every check runs before the first write, and a
+// failed kernel stops the stream before the copy-out.
 template <class W>
 static bool run_host(W* ws, const Geom& g, bool square, u64* dst, const u64* a, const u64* b) {
     const size_t out_bytes = g.out_len * sizeof(u64);
-    if (!ws->a.ensure(g.la * 8) || (!square && !ws->b.ensure(g.lb * 8)) || !ws->out.ensure(out_bytes) ||
+    u64* direct = (u64*)mapped_host_pointer(dst);
+    if (!ws->a.ensure(g.la * 8) || (!square && !ws->b.ensure(g.lb * 8)) || (!direct && !ws->out.ensure(out_bytes)) ||
         !ws->scratch.ensure(g.scratch_bytes(square)))
         return false;
     cudaStream_t st = ws->stream;
     if (!cuda_ok(cudaMemcpyAsync(ws->a.ptr, a, g.la * 8, cudaMemcpyHostToDevice, st), "copy a")) return false;
-    if (!square && !cuda_ok(cudaMemcpyAsync(ws->b.ptr, b, g.lb * 8, cudaMemcpyHostToDevice, st), "copy b"))
+    cudaEvent_t b_ready = nullptr;
+    if (!square) {
+        if (!cuda_ok(cudaMemcpyAsync(ws->b.ptr, b, g.lb * 8, cudaMemcpyHostToDevice, ws->upload), "copy b") ||
+            !cuda_ok(cudaEventRecord(ws->b_ready, ws->upload), "cudaEventRecord"))
+            return false;
+        b_ready = ws->b_ready;
+    }
+    u64* out = direct ? direct : (u64*)ws->out.ptr;
+    if (!execute(g, square, (const u64*)ws->a.ptr, (const u64*)ws->b.ptr, out, ws->scratch.ptr, st, b_ready))
         return false;
-    if (!execute(g, square, (const u64*)ws->a.ptr, (const u64*)ws->b.ptr, (u64*)ws->out.ptr, ws->scratch.ptr, st))
+    if (!direct && !cuda_ok(cudaMemcpyAsync(dst, out, out_bytes, cudaMemcpyDeviceToHost, st), "copy dst"))
         return false;
-    if (!cuda_ok(cudaStreamSynchronize(st), "kernels")) return false;
-    if (!cuda_ok(cudaMemcpyAsync(dst, ws->out.ptr, out_bytes, cudaMemcpyDeviceToHost, st), "copy dst")) return false;
-    return cuda_ok(cudaStreamSynchronize(st), "copy dst");
+    return cuda_ok(cudaStreamSynchronize(st), "kernels");
 }
 
 extern "C" {

@@ -51,6 +51,8 @@ struct TransformArgs {
     int vstride_col;   // padded words per column vector in shared memory
     int s_bits;        // low-digit bits of the two-level four-step twiddle tables
     int wide;          // 1: primes up to 2^31 in canonical arithmetic; 0: lazy, p < 2^30
+    int op_base;       // first operand of a single-member column pass (0: a, 1: b)
+    int op_count;      // operands of that pass; 0 means every operand of the member
     PrimeSet ps;
 };
 

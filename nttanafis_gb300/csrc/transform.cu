@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
     // grid.z: operands (1 or 2) of one member, or 2 per member in a batch
-    const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z;
+    const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z + g.op_base;
     const Member m = member_of(g, g.batch ? (blockIdx.z >> 1) : 0, false);
     if (op && m.square) return;
     const PrimeParams& pp = g.ps.pr[prime];
@@ -317,7 +317,8 @@ template <class A, int L>
 static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
     if (init) return opt_in(k, NTT_COLS_CARVEOUT);
-    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : (square ? 1 : 2));
+    const unsigned ops = g.op_count ? g.op_count : (square ? 1 : 2);
+    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : ops);
     const size_t smem = col_smem(L);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
