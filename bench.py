@@ -455,8 +455,7 @@ def run_gpu(args) -> None:
 
     # Per-kernel device times: events recorded between the library's launches.
     kernel_names = ["pack+column DIF (k_fwd_cols)", "row DIF+pointwise+DIT (k_rows)",
-                    "column DIT (k_inv_cols)", "CRT+window+tile carry (k_crt_mul)",
-                    "tile carry scan and apply (k_carry)"]
+                    "column DIT (k_inv_cols)", "CRT+window sums+look-back carry (k_crt_mul)"]
     import ctypes
 
     reps = 10
@@ -503,7 +502,8 @@ def run_gpu(args) -> None:
                      "unit_of_launch": "one product (the fused kernel sequence below)",
                      "dominant_kernel": kernel_names[dominant] if dominant is not None else None},
         "kernels": kernels, "kernels_ms_total": instrumented_ms,
-        "gpu_launches": launches, "wall_s": t_wall, "parity": {"fingerprint_ok": fingerprint_ok},
+        "gpu_launches": launches, "wall_s": t_wall,
+        "parity": {"fingerprint_ok": fingerprint_ok, "lookback_timeouts": ntt.lookback_timeouts()},
     }
     line["clocks"] = sampler.summary()
     if rank == 0 and not args.no_configs:

@@ -197,6 +197,11 @@ uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const uint64_t* 
 int ntt_timing_start(int count);
 int ntt_timing_stop(float* ms, int capacity);
 
+/* Look-back waits of the CRT carry scan that gave up since the library was loaded
+ * (each wait is bounded; a nonzero count means a result may be wrong). Synchronizes
+ * the device. */
+uint32_t ntt_lookback_timeouts(void);
+
 /* Message of the last failure on this thread ("" when none). */
 const char* ntt_last_error(void);
 /* Kernels launched by this process since load (counted per launch by the host). */

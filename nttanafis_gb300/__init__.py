@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     exported_symbols,
     kernel_launches,
     last_error,
+    lookback_timeouts,
     library,
 )
 from .operands import operand  # noqa: F401

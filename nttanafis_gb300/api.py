@@ -99,6 +99,7 @@ _SIGNATURES = [
       ctypes.c_void_p]),
     ("ntt_timing_start", ctypes.c_int, [ctypes.c_int]),
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    ("ntt_lookback_timeouts", ctypes.c_uint32, []),
     ("ntt_last_error", ctypes.c_char_p, []),
     ("ntt_kernel_launches", ctypes.c_uint64, []),
     ("ntt_version", ctypes.c_char_p, []),
@@ -136,6 +137,11 @@ def last_error() -> str:
 
 def kernel_launches() -> int:
     return int(library().ntt_kernel_launches())
+
+
+def lookback_timeouts() -> int:
+    """Bounded look-back waits of the CRT carry scan that gave up (expected 0)."""
+    return int(library().ntt_lookback_timeouts())
 
 
 def _host(arr: np.ndarray, name: str) -> np.ndarray:

@@ -439,6 +439,11 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
     ta.np = g.np;
     ta.log_t = g.log_t;
     ta.wide = g.wide;
+    const u64 spec_bytes = (g.spec_words(square) * 4 + 255) & ~(u64)255;
+    if (!g.conv) {
+        ta.flags = (u32*)((uint8_t*)scratch + spec_bytes);
+        ta.flag_words = (u32)carry_flag_words(g.out_len);
+    }
     const bool sign = g.sign != 0;
     if (g.log_t <= kMaxBlockLog) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
@@ -480,8 +485,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         mark(st);
         return ok;
     }
-    const u64 spec_bytes = (g.spec_words(square) * 4 + 255) & ~(u64)255;
-    g_launches += 2;
+    g_launches += 1;
     return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst,
                                   (uint8_t*)scratch + spec_bytes, cp, st, mark),
                    "CRT launch");
@@ -984,7 +988,7 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         d.conv_len = m.g.conv_len;
         d.dst = r.dst;
         d.out_len = m.g.out_len;
-        d.agg = arena + m.offset + ((m.g.spec_words(m.square) * 4 + 255) & ~(u64)255);
+        d.agg = m.g.conv ? nullptr : arena + m.offset + ((m.g.spec_words(m.square) * 4 + 255) & ~(u64)255);
         d.square = m.square ? 1u : 0u;
         d.stride = (u32)m.g.stride;
     }
@@ -1048,7 +1052,7 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         } else {
             u64 max_out = 0;
             for (size_t i = k; i < end; ++i) max_out = std::max(max_out, members[i].g.out_len);
-            g_launches += 2;
+            g_launches += 1;
             if (!cuda_ok(launch_crt_mul_batch(dev_desc + k, n, (int)((max_out + kCrtTile - 1) / kCrtTile), g0.log_t,
                                               cp, st),
                          "batched CRT launch"))
@@ -1058,6 +1062,8 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
     }
     return 1;
 }
+
+uint32_t ntt_lookback_timeouts(void) { return lookback_timeouts(); }
 
 const char* ntt_last_error(void) { return g_error.c_str(); }
 uint64_t ntt_kernel_launches(void) { return g_launches.load(); }

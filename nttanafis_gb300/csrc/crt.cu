@@ -11,9 +11,9 @@
 // k lands at limb k and spans l64 limbs. One CTA owns 1024 output limbs: it
 // reconstructs the coefficients that reach them, sums the overlapping windows,
 // propagates carries inside the tile with a generate/propagate block scan and
-// records the tile's (generate, propagate) pair. A one-CTA scan then resolves the
-// carry into every tile and a third kernel applies it (at most a run of all-ones
-// limbs). No kernel waits on another CTA.
+// resolves the tile's carry-in with a decoupled look-back over the earlier tiles'
+// published (generate, propagate) pairs, so the limbs are written once, final.
+// Every look-back wait is bounded; a wait that gives up is counted and flagged.
 #include "launch.h"
 
 namespace ntt {
@@ -139,10 +139,44 @@ __device__ __forceinline__ void warp_scan_gp(u32& g, u32& p) {
 // word planes, so a warp reads consecutive 64-bit words. Warp w owns limbs
 // [128w, 128w + 128) of the tile; lane l handles limbs 32c + l of them (c < 4),
 // so every shared and global access of a warp is to consecutive words.
+// Look-back state of a tile: bits 0-1 the state, bit 2 the generate bit (or, for
+// an inclusive state, the carry out of every tile up to this one), bit 3 the
+// propagate bit.
+constexpr u32 kTileAggregate = 1, kTileInclusive = 2;
+// Spins (about 64 ns each) before a look-back gives up: far above any real wait.
+constexpr u32 kMaxSpins = 1u << 20;
+// Look-back waits that gave up since the library was loaded (none expected).
+__device__ u32 g_lookback_timeouts;
+
+// The carry out of tiles 0..t-1: walks back from tile t-1, composing aggregates
+// until it meets an inclusive state. Tile 0 always publishes an inclusive state,
+// so the walk ends. Returns false if a wait exceeded kMaxSpins.
+__device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin) {
+    u32 ga = 0, pa = 1;  // composite of the tiles after the current one, up to t-1
+    for (int j = (int)t - 1; j >= 0; --j) {
+        u32 s, spins = 0;
+        while (((s = status[j]) & 3u) == 0) {
+            if (++spins > kMaxSpins) return false;
+            __nanosleep(64);
+        }
+        const u32 gj = (s >> 2) & 1u, pj = (s >> 3) & 1u;
+        if ((s & 3u) == kTileInclusive) {
+            cin = ga | (pa & gj);
+            return true;
+        }
+        ga = ga | (pa & gj);
+        pa = pa & pj;
+    }
+    cin = ga;  // not reached: tile 0 is inclusive
+    return true;
+}
+
+// flags: [0] tile counter, [1] error word, [2 + t] look-back state of tile t; all
+// zero when the kernel starts (the preceding transform kernel clears them).
 template <int NP>
 __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__ resid, int log_t,
                                                           u64 conv_len, u64 out_len, u64* __restrict__ dst,
-                                                          uint8_t* __restrict__ agg,
+                                                          u32* __restrict__ flags,
                                                           const __grid_constant__ CrtParams cp,
                                                           const ProductDesc* __restrict__ batch) {
     if (batch) {  // member blockIdx.y of a batch: grid.x covers its largest member
@@ -151,15 +185,22 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
         conv_len = d.conv_len;
         out_len = d.out_len;
         dst = d.dst;
-        agg = d.agg;
-        if ((u64)blockIdx.x * kCrtTile >= out_len) return;
+        flags = reinterpret_cast<u32*>(d.agg);
     }
+    // Tiles are numbered in the order CTAs start, so a tile only ever waits for
+    // tiles whose CTAs are already running.
+    __shared__ u32 s_tile, s_cin;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
+    __syncthreads();
+    const u32 tile = s_tile;
+    const u32 tiles = (u32)((out_len + kCrtTile - 1) / kCrtTile);
+    if (tile >= tiles) return;
     constexpr int kBack = 4;  // coefficients before the tile that reach into it (l64 <= 4)
     constexpr int kWords = kCrtTile + kBack;
     constexpr int kChunks = kCrtTile / (32 * (kCrtThreads / 32));  // 4 chunks of 32 limbs per warp
     __shared__ u64 xs[4][kWords];
     __shared__ u32 wsum_g[32], wsum_p[32];
-    const u64 j0 = (u64)blockIdx.x * kCrtTile;
+    const u64 j0 = (u64)tile * kCrtTile;
     for (int kk = threadIdx.x; kk < kWords; kk += kCrtThreads) {
         const int64_t k = (int64_t)j0 - kBack + kk;
         u64 w[4] = {0, 0, 0, 0};
@@ -214,8 +255,30 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
     }
     if (lane == 0) { wsum_g[warp] = WG; wsum_p[warp] = WP; }
     __syncthreads();
-    // carry into this warp's first limb when the tile's carry-in is zero
-    u32 cin = 0;
+    if (threadIdx.x == 0) {
+        u32 tg = 0, tp = 1;  // the tile's (generate, propagate) pair
+        for (int w = 0; w < kCrtThreads / 32; ++w) {
+            u32 g = wsum_g[w], p = wsum_p[w];
+            compose(g, p, tg, tp);
+            tg = g;
+            tp = p;
+        }
+        u32* status = flags + 2;
+        u32 cin = 0;
+        if (tile > 0) {
+            atomicExch(status + tile, kTileAggregate | (tg << 2) | (tp << 3));
+            if (!look_back(status, tile, cin)) {
+                atomicAdd(&g_lookback_timeouts, 1u);
+                atomicOr(&flags[1], 1u);
+                cin = 0;
+            }
+        }
+        atomicExch(status + tile, kTileInclusive | ((tg | (tp & cin)) << 2));
+        s_cin = cin;
+    }
+    __syncthreads();
+    // carry into this warp's first limb: the tile's carry-in through earlier warps
+    u32 cin = s_cin;
     for (int w = 0; w < warp; ++w) cin = wsum_g[w] | (wsum_p[w] & cin);
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
@@ -223,83 +286,6 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
         const u32 carry = eg[c] | (ep[c] & cin);
         if (j < out_len) dst[j] = r[c] + carry;
         cin = cg[c] | (cpp[c] & cin);
-    }
-    if (threadIdx.x == kCrtThreads - 1) {
-        u32 tg = 0, tp = 1;
-        for (int w = 0; w < kCrtThreads / 32; ++w) {
-            u32 g = wsum_g[w], p = wsum_p[w];
-            compose(g, p, tg, tp);
-            tg = g;
-            tp = p;
-        }
-        agg[blockIdx.x] = (uint8_t)(tg | (tp << 1));
-    }
-}
-
-// One CTA: resolves the carry into every tile (cin[t] = carry out of tiles
-// 0..t-1), then adds it. A tile with carry-in one is incremented at its first
-// limb that is not all ones; the all-ones limbs below it become zero. Warps take
-// such tiles in turn; random operands almost never produce one.
-__global__ void __launch_bounds__(1024) k_carry(const uint8_t* __restrict__ agg, uint8_t* __restrict__ cin,
-                                                int tiles, u64* __restrict__ dst, u64 out_len,
-                                                const ProductDesc* __restrict__ batch) {
-    if (batch) {  // one CTA per member
-        const ProductDesc& d = batch[blockIdx.x];
-        out_len = d.out_len;
-        tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
-        agg = d.agg;
-        cin = d.agg + tiles;
-        dst = d.dst;
-    }
-    constexpr int kList = 1024;
-    __shared__ int s_count;
-    __shared__ int s_list[kList];
-    if (threadIdx.x == 0) s_count = 0;
-    const int per = (tiles + blockDim.x - 1) / blockDim.x;
-    const int t0 = threadIdx.x * per;
-    uint8_t mine[8];  // this thread's aggregates (per <= 8 for up to 8192 tiles)
-    u32 G = 0, P = 1;
-    for (int t = t0, i = 0; t < t0 + per && t < tiles; ++t, ++i) {
-        const uint8_t a = agg[t];
-        if (i < 8) mine[i] = a;
-        u32 g = a & 1u, p = (a >> 1) & 1u;
-        compose(g, p, G, P);
-        G = g;
-        P = p;
-    }
-    u32 tg, tp;
-    block_scan_gp(G, P, tg, tp);  // its barriers also order s_count's initialisation
-    u32 c = G;
-    for (int t = t0, i = 0; t < t0 + per && t < tiles; ++t, ++i) {
-        cin[t] = (uint8_t)c;
-        if (c) {
-            const int slot = atomicAdd(&s_count, 1);
-            if (slot < kList) s_list[slot] = t;
-        }
-        const uint8_t a = i < 8 ? mine[i] : agg[t];
-        c = (a & 1u) | (((a >> 1) & 1u) & c);
-    }
-    __syncthreads();
-    const int count = s_count;
-    if (count == 0) return;  // the usual case: no tile receives a carry
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int work = count <= kList ? count : tiles;
-    for (int i = warp; i < work; i += nwarps) {
-        const int t = count <= kList ? s_list[i] : i;
-        if (!cin[t]) continue;
-        const u64 begin = (u64)t * kCrtTile;
-        const u64 end = min(begin + (u64)kCrtTile, out_len);
-        for (u64 base = begin; base < end; base += 32) {
-            const u64 j = base + lane;
-            const bool ones = j >= end || dst[j] == ~0ull;
-            const unsigned stop = __ballot_sync(0xffffffffu, !ones);
-            const int first = stop ? __ffs(stop) - 1 : 32;
-            if (j < end) {
-                if (lane < first) dst[j] = 0;
-                else if (lane == first) dst[j] += 1;
-            }
-            if (stop) break;
-        }
     }
 }
 
@@ -364,9 +350,8 @@ template <int NP>
 static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
                        const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
     const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
-    k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst, agg, cp, nullptr);
-    if (mark) mark(st);
-    k_carry<<<1, 1024, 0, st>>>(agg, agg + tiles, tiles, dst, out_len, nullptr);
+    k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst,
+                                                  reinterpret_cast<u32*>(agg), cp, nullptr);
     if (mark) mark(st);
 }
 
@@ -375,7 +360,6 @@ static void crt_mul_batch_np(const ProductDesc* batch, int count, int max_tiles,
                              cudaStream_t st) {
     k_crt_mul<NP><<<dim3(max_tiles, count), kCrtThreads, 0, st>>>(nullptr, log_t, 0, 0, nullptr, nullptr, cp,
                                                                    batch);
-    k_carry<<<count, 1024, 0, st>>>(nullptr, nullptr, 0, nullptr, 0, batch);
 }
 
 cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_tiles, int log_t,
@@ -455,5 +439,11 @@ cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u
 }
 
 cudaError_t init_crt_kernels() { return cudaSuccess; }
+
+u32 lookback_timeouts() {
+    u32 n = 0;
+    if (cudaMemcpyFromSymbol(&n, g_lookback_timeouts, sizeof(n)) != cudaSuccess) return ~0u;
+    return n;
+}
 
 }  // namespace ntt

@@ -28,7 +28,7 @@ struct ProductDesc {
     u64 conv_len;
     u64* dst;
     u64 out_len;       // limbs of a product
-    uint8_t* agg;      // carry flags of a product (2 bytes per output tile)
+    uint8_t* agg;      // CRT look-back flags of a product (carry_flag_words u32), or null
     u32 square;
     u32 stride;        // convolution limbs per coefficient
 };
@@ -53,6 +53,8 @@ struct TransformArgs {
     int wide;          // 1: primes up to 2^31 in canonical arithmetic; 0: lazy, p < 2^30
     int op_base;       // first operand of a single-member column pass (0: a, 1: b)
     int op_count;      // operands of that pass; 0 means every operand of the member
+    u32* flags;        // CRT look-back flags to clear (products), or null
+    u32 flag_words;
     PrimeSet ps;
 };
 
@@ -88,11 +90,12 @@ cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_c
                                   const CrtParams& cp, cudaStream_t st);
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
                                    int stride, bool sign, cudaStream_t st);
-// Scratch bytes the CRT carry pass needs for `out_len` output limbs.
-inline u64 carry_scratch_bytes(u64 out_len) {
-    const u64 tiles = (out_len + kCrtTile - 1) / kCrtTile;
-    return 2 * tiles + 16;
-}
+// Scratch bytes of the CRT look-back flags for `out_len` output limbs: a tile
+// counter, an error word and one state word per tile of kCrtTile limbs.
+__host__ __device__ inline u64 carry_flag_words(u64 out_len) { return 2 + (out_len + kCrtTile - 1) / kCrtTile; }
+inline u64 carry_scratch_bytes(u64 out_len) { return 4 * carry_flag_words(out_len); }
+// Look-back waits that gave up since load (0 unless the GPU misbehaved).
+u32 lookback_timeouts();
 
 // Sets the message returned by ntt_last_error() on this thread.
 void set_last_error(const std::string& message);

@@ -45,7 +45,7 @@ constexpr int kNaPrimes = 5;
 // most 2^20 limbs, so it holds every product this path admits.
 constexpr u32 kNaPrime[kNaPrimes] = {1012924417u, 1004535809u, 998244353u, 985661441u, 975175681u};
 constexpr size_t kNaSpecWords = (size_t)2 * kNaPrimes * kNaPoints;
-constexpr size_t kNaFlagWords = 64;  // carry flags of at most 5 output tiles, 2 bytes each
+constexpr size_t kNaFlagWords = 64;  // CRT look-back flags: 2 + at most 5 output tiles
 constexpr size_t kNaRootEntries = (size_t)2 * kNaPrimes * kNaPoints;
 
 }  // namespace
@@ -251,6 +251,8 @@ extern "C" uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const
     ta.np = kNaPrimes;
     ta.log_t = log_t;
     ta.wide = 0;
+    ta.flags = d->scratch + kNaSpecWords;  // cleared by the transform kernel of this call
+    ta.flag_words = (u32)carry_flag_words(out_len);
     for (int i = 0; i < kNaPrimes; ++i) {
         PrimeParams pp = g_na_params[i];
         pp.scale = g_na_scale[i][log_t];

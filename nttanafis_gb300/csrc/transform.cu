@@ -64,8 +64,20 @@ __device__ __forceinline__ Member member_of(const TransformArgs& g, int idx, boo
     return Member{g.a, g.b, g.la, g.lb, g.spec, g.conv_len, square};
 }
 
+// Clears the CRT look-back flags of a member (products only; see k_crt_mul).
+__device__ __forceinline__ void clear_flags(const TransformArgs& g, int idx) {
+    u32* f = g.flags;
+    u32 n = g.flag_words;
+    if (g.batch) {
+        const ProductDesc& d = g.batch[idx];
+        f = reinterpret_cast<u32*>(d.agg);
+        n = f ? (u32)carry_flag_words(d.out_len) : 0u;
+    }
+    for (u32 i = threadIdx.x; i < n; i += blockDim.x) f[i] = 0;
+}
+
 // One CTA transforms one prime: pack, forward a (and b), pointwise, inverse, scale.
-// grid = (np, members).
+// grid = (np, members). The prime-0 CTA of a member also clears its CRT flags.
 template <class A, bool SQUARE, bool SIGNED, int LOG_N>
 __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
@@ -73,6 +85,7 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     constexpr int VS = padded_len(N);
     const PrimeParams& pp = g.ps.pr[blockIdx.x];
     const Member m = member_of(g, blockIdx.y, SQUARE);
+    if (blockIdx.x == 0) clear_flags(g, blockIdx.y);
     u32* sa = sm;
     u32* sb = sm + VS;
     for (int i = threadIdx.x; i < N; i += kThreads) {
@@ -244,6 +257,7 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ T
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, false);
+    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
     const u64 step = (u64)M::RS << g.log_c;
     u32* const base = m.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
                       (blockIdx.x << M::LOG_G) + M::col();

@@ -187,3 +187,8 @@ def test_device_and_plan_scratch_paths(gpu):
     torch.cuda.synchronize()
     assert bool((dst == -1).all())
     w.close()
+
+
+def test_no_lookback_timeouts(gpu):
+    # every bounded look-back wait of the CRT carry scan completed
+    assert gpu.lookback_timeouts() == 0
