@@ -255,8 +255,8 @@ struct PrimeTables {
     uint2* inv = nullptr;
 };
 struct StepTables {
-    uint2* f_lo = nullptr;
-    uint2* f_hi = nullptr;
+    uint2* f_a = nullptr;
+    uint2* f_b = nullptr;
     uint2* i_lo = nullptr;
     uint2* i_hi = nullptr;
     uint2 scale{0, 0};
@@ -309,8 +309,15 @@ static bool prime_tables(int dev, u32 p, PrimeTables& out) {
     return true;
 }
 
-static int s_bits_of(int log_t) { return (log_t + 1) / 2; }
+static u32 bit_reverse(u32 x, int bits) {
+    u32 r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((x >> b) & 1u) << (bits - 1 - b);
+    return r;
+}
 
+// Root tables of one transform length: the inverse scale and, for the four-step
+// sizes, the forward and inverse twiddle factors in the layouts the column and row
+// passes read (launch.h describes them).
 static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
     auto key = std::make_tuple(dev, p, log_t);
     auto it = g_step_tables.find(key);
@@ -323,26 +330,31 @@ static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
     StepTables t;
     t.scale = shoup_pair(scale, p);
     if (log_t > kMaxBlockLog) {
-        const int s = s_bits_of(log_t);
-        const int nlo = 1 << s, nhi = 1 << (log_t - s);
-        std::vector<uint2> flo(nlo), ilo(nlo), fhi(nhi), ihi(nhi);
-        u32 x = 1, ix = 1;
-        for (int e = 0; e < nlo; ++e) {
-            flo[e] = shoup_pair(x, p);
-            ilo[e] = shoup_pair(ix, p);
-            x = mulmod(x, w, p);
-            ix = mulmod(ix, iw, p);
+        const int log_r = log_t / 2, log_c = log_t - log_r;
+        const u64 R = (u64)1 << log_r, C = (u64)1 << log_c;
+        const u64 RS = (u64)1 << kColLogRS, SW = R / RS;
+        const u64 NL = (u64)1 << kRowTwLoBits, NH = C >> kRowTwLoBits;
+        std::vector<uint2> fa(C * RS), fb(C * SW), ilo(R * NL), ihi(R * NH);
+        const u32 w_sw = powmod(w, SW, p);
+        u32 wc = 1, wc_sw = 1;  // w^col and w^(col * SW)
+        for (u64 col = 0; col < C; ++col) {
+            u32 x = 1;
+            for (u64 u = 0; u < RS; ++u, x = mulmod(x, wc_sw, p)) fa[col * RS + u] = shoup_pair(x, p);
+            x = 1;
+            for (u64 j = 0; j < SW; ++j, x = mulmod(x, wc, p)) fb[col * SW + j] = shoup_pair(x, p);
+            wc = mulmod(wc, w, p);
+            wc_sw = mulmod(wc_sw, w_sw, p);
         }
-        const u32 ws = powmod(w, (u64)1 << s, p), iws = powmod(iw, (u64)1 << s, p);
-        x = 1;
-        ix = scale;
-        for (int e = 0; e < nhi; ++e) {
-            fhi[e] = shoup_pair(x, p);
-            ihi[e] = shoup_pair(ix, p);
-            x = mulmod(x, ws, p);
-            ix = mulmod(ix, iws, p);
+        for (u64 row = 0; row < R; ++row) {
+            const u32 c = powmod(iw, bit_reverse((u32)row, log_r), p);  // w^-k1
+            u32 x = 1;
+            for (u64 lo = 0; lo < NL; ++lo, x = mulmod(x, c, p))
+                ilo[row * NL + 16 * (lo & 3) + (lo >> 2)] = shoup_pair(x, p);
+            const u32 c64 = x;  // w^(-k1 * 64)
+            x = scale;
+            for (u64 hi = 0; hi < NH; ++hi, x = mulmod(x, c64, p)) ihi[row * NH + hi] = shoup_pair(x, p);
         }
-        if (!upload(&t.f_lo, flo) || !upload(&t.f_hi, fhi) || !upload(&t.i_lo, ilo) || !upload(&t.i_hi, ihi))
+        if (!upload(&t.f_a, fa) || !upload(&t.f_b, fb) || !upload(&t.i_lo, ilo) || !upload(&t.i_hi, ihi))
             return false;
     }
     g_step_tables[key] = t;
@@ -393,8 +405,8 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
         pp.scale = st.scale;
         pp.fwd = pt.fwd;
         pp.inv = pt.inv;
-        pp.f4_lo = st.f_lo;
-        pp.f4_hi = st.f_hi;
+        pp.f4_a = st.f_a;
+        pp.f4_b = st.f_b;
         pp.i4_lo = st.i_lo;
         pp.i4_hi = st.i_hi;
         // CRT cofactors M_i = P / p_i and their inverses.
@@ -459,7 +471,6 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         const int target = 32 / G;
         vs += ((target - vs) % 32 + 32) % 32;
         ta.vstride_col = vs;
-        ta.s_bits = s_bits_of(g.log_t);
         if (b_ready && !square) {
             g_launches += 1;
             ta.op_count = 1;
@@ -1036,7 +1047,6 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         } else {
             ta.log_r = g0.log_t / 2;
             ta.log_c = g0.log_t - ta.log_r;
-            ta.s_bits = s_bits_of(g0.log_t);
             g_launches += 3;
             if (!cuda_ok(launch_fwd_cols(ta, false, sign, st), "batched column pass launch") ||
                 !cuda_ok(launch_rows(ta, false, st), "batched row pass launch") ||

@@ -135,10 +135,6 @@ __device__ __forceinline__ void warp_scan_gp(u32& g, u32& p) {
     }
 }
 
-// Tile of kCrtTile output limbs. Coefficient words sit in shared memory as four
-// word planes, so a warp reads consecutive 64-bit words. Warp w owns limbs
-// [128w, 128w + 128) of the tile; lane l handles limbs 32c + l of them (c < 4),
-// so every shared and global access of a warp is to consecutive words.
 // Look-back state of a tile: bits 0-1 the state, bit 2 the generate bit (or, for
 // an inclusive state, the carry out of every tile up to this one), bit 3 the
 // propagate bit.
@@ -149,8 +145,9 @@ constexpr u32 kMaxSpins = 1u << 20;
 __device__ u32 g_lookback_timeouts;
 
 // The carry out of tiles 0..t-1: walks back from tile t-1, composing aggregates
-// until it meets an inclusive state. Tile 0 always publishes an inclusive state,
-// so the walk ends. Returns false if a wait exceeded kMaxSpins.
+// until it meets an inclusive state or the composite stops propagating (almost
+// always at tile t-1). Tile 0 always publishes an inclusive state, so the walk
+// ends. Returns false if a wait exceeded kMaxSpins.
 __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin) {
     u32 ga = 0, pa = 1;  // composite of the tiles after the current one, up to t-1
     for (int j = (int)t - 1; j >= 0; --j) {
@@ -166,11 +163,19 @@ __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin)
         }
         ga = ga | (pa & gj);
         pa = pa & pj;
+        if (!pa) {  // tiles j..t-1 do not propagate: their carry out is known
+            cin = ga;
+            return true;
+        }
     }
     cin = ga;  // not reached: tile 0 is inclusive
     return true;
 }
 
+// Tile of kCrtTile output limbs. Coefficient words sit in shared memory as four
+// word planes, so a warp reads consecutive 64-bit words. Warp w owns limbs
+// [128w, 128w + 128) of the tile; lane l handles limbs 32c + l of them (c < 4),
+// so every shared and global access of a warp is to consecutive words.
 // flags: [0] tile counter, [1] error word, [2 + t] look-back state of tile t; all
 // zero when the kernel starts (the preceding transform kernel clears them).
 template <int NP>

@@ -17,6 +17,27 @@ constexpr int kMaxLogT = 25;
 // Output limbs per CTA of the CRT + carry kernel.
 constexpr int kCrtTile = 1024;
 
+// Column passes of the four-step: a CTA of kColThreads threads owns 2^kColLogG
+// columns; thread t takes column t mod 2^kColLogG and rows r0 + k * RS with
+// r0 = t >> kColLogG, RS = 2^kColLogRS rows per sweep, k < SW = R / RS.
+#ifndef NTT_COLS_LOG_G
+#define NTT_COLS_LOG_G 3
+#endif
+constexpr int kColThreads = 256;
+constexpr int kColLogG = NTT_COLS_LOG_G;
+constexpr int kColLogRS = 8 - kColLogG;
+// Four-step twiddles, tabulated per prime and transform length T = R * C:
+//  - forward, applied by the column pass: w_T^(col * brev(row)). Row r0 + RS*k has
+//    the bit-reversed index brev(r0) * SW + brev(k), so the twiddle is
+//    f4_a[col * RS + brev(r0)] = w_T^(col * brev(r0) * SW) (one per thread) times
+//    f4_b[col * SW + brev(k)] = w_T^(col * brev(k)) (one per sweep);
+//  - inverse, applied by the row pass: w_T^(-k1 * n2) times the inverse scale for
+//    the row of frequency k1 = brev(row) and n2 = 64 * hi + lo, as
+//    i4_lo[row * 64 + 16 * (lo mod 4) + lo / 4] = w_T^(-k1 * lo) (ordered so that a
+//    warp's reads of consecutive 4-element groups hit consecutive words) times
+//    i4_hi[row * C / 64 + hi] = w_T^(-k1 * 64 * hi) * scale.
+constexpr int kRowTwLoBits = 6;
+
 // One product or convolution of a batch, read by the kernels from device memory.
 // All members of one launch share the transform length, the primes and the sign
 // mode; everything else varies per member.
@@ -49,7 +70,6 @@ struct TransformArgs {
     int log_r, log_c;  // four-step split T = R * C (unused on the one-CTA path)
     int log_g;         // log2 columns per CTA in the column passes
     int vstride_col;   // padded words per column vector in shared memory
-    int s_bits;        // low-digit bits of the two-level four-step twiddle tables
     int wide;          // 1: primes up to 2^31 in canonical arithmetic; 0: lazy, p < 2^30
     int op_base;       // first operand of a single-member column pass (0: a, 1: b)
     int op_count;      // operands of that pass; 0 means every operand of the member

@@ -114,10 +114,10 @@ struct PrimeParams {
     uint2 scale;     // small-path inverse scale T^-1 * (P/p)^-1 * 2^32 with companion
     const uint2* fwd;    // level-major forward roots: fwd[h + j] = w_{2h}^j
     const uint2* inv;    // level-major inverse roots: inv[h + j] = w_{2h}^-j
-    const uint2* f4_lo;  // four-step twiddles w_T^e, low digit of e
-    const uint2* f4_hi;  //                      high digit of e
-    const uint2* i4_lo;  // inverse four-step twiddles w_T^-e, low digit
-    const uint2* i4_hi;  // high digit, times the inverse scale
+    const uint2* f4_a;   // forward four-step twiddles: per column-pass thread
+    const uint2* f4_b;   //                              per column and sweep
+    const uint2* i4_lo;  // inverse four-step twiddles: per row, low digit of n2
+    const uint2* i4_hi;  //                             per row, high digit, times the scale
 };
 
 constexpr int kMaxPrimes = 8;

@@ -21,19 +21,33 @@
 
 namespace ntt {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kColThreads;
 #ifndef NTT_ROW_THREADS
 #define NTT_ROW_THREADS 128
 #endif
-#ifndef NTT_COLS_LOG_G
-#define NTT_COLS_LOG_G 3
+// Minimum resident CTAs per SM requested from the register allocator (0: none).
+#ifndef NTT_COLS_MINB
+#define NTT_COLS_MINB 0
+#endif
+#ifndef NTT_ROWS_MINB
+#define NTT_ROWS_MINB 0
+#endif
+#if NTT_COLS_MINB > 0
+#define NTT_COLS_BOUNDS __launch_bounds__(kThreads, NTT_COLS_MINB)
+#else
+#define NTT_COLS_BOUNDS __launch_bounds__(kThreads)
+#endif
+#if NTT_ROWS_MINB > 0
+#define NTT_ROWS_BOUNDS __launch_bounds__(kRowThreads, NTT_ROWS_MINB)
+#else
+#define NTT_ROWS_BOUNDS __launch_bounds__(kRowThreads)
 #endif
 // Threads of a row-pass CTA.
 constexpr int kRowThreads = NTT_ROW_THREADS;
 
 // log2 of the columns one CTA of a column pass owns: 8 columns, so a row segment
 // is one 32-byte sector of u32 residues (two of u64 limbs).
-__host__ __device__ constexpr int col_group_log(int) { return NTT_COLS_LOG_G; }
+__host__ __device__ constexpr int col_group_log(int) { return kColLogG; }
 // Padded words per column in shared memory: congruent to 32/G mod 32 so that a
 // warp's G columns times 32/G rows fall in distinct banks.
 __host__ __device__ constexpr int col_vstride(int log_r) {
@@ -140,7 +154,7 @@ struct ColumnMap {
 };
 
 template <class A, bool SIGNED, int LOG_R>
-__global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ TransformArgs g) {
+__global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     using M = ColumnMap<LOG_R>;
     constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;  // sweeps per batch; B*RS is a multiple of 32
@@ -164,6 +178,15 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
     u32* s = sm + M::slot0();
     uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
     load_table<LOG_R>(tw, pp.fwd);
+    // Per-sweep four-step factors of the CTA's columns, rows padded to SW + 1 entries
+    // so that the G columns of a warp read distinct banks.
+    uint2* fb = tw + (1 << LOG_R);
+    {
+        const uint2* src = pp.f4_b + ((size_t)(blockIdx.x << M::LOG_G) << M::LOG_SW);
+        for (int i = threadIdx.x; i < (M::G << M::LOG_SW); i += kThreads)
+            fb[(i >> M::LOG_SW) * (M::SWEEPS + 1) + (i & (M::SWEEPS - 1))] = __ldg(src + i);
+    }
+    const uint2 fa = __ldg(pp.f4_a + ((size_t)col << kColLogRS) + (__brev((u32)r0) >> (32 - kColLogRS)));
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
         u64 x[B];
@@ -176,20 +199,18 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
     }
     __syncthreads();
     dif_full<A, LOG_R, kThreads>(sm, M::G, M::VS, tw, pp.p);
-    // Four-step twiddle w_T^(col * k1) with k1 = bitrev(row), then the store.
+    // Four-step twiddle w_T^(col * brev(row)) = fa * fb[col][brev(k)], then the store.
     u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
-    const u32 lo_mask = (1u << g.s_bits) - 1;
-    const u32 e0 = col * (__brev((u32)r0) >> (32 - LOG_R));
+    const uint2* fbc = fb + M::col() * (M::SWEEPS + 1);
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
-        const u32 ek = e0 + col * (__brev((u32)k0) >> (32 - M::LOG_SW));
+        const uint2* fk = fbc + (__brev((u32)k0) >> (32 - M::LOG_SW));
         const u32* sk = s + slot_offset<M::RS>(k0);
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-            const u32 ex = ek + col * M::brev_sweep(u);
             u32 x = sk[slot_offset<M::RS>(u)];
-            x = A::mulc(x, __ldg(pp.f4_lo + (ex & lo_mask)), pp.p);
-            x = A::mulc(x, __ldg(pp.f4_hi + (ex >> g.s_bits)), pp.p);
+            x = A::mulc(x, fk[M::brev_sweep(u)], pp.p);
+            x = A::mulc(x, fa, pp.p);
             dst[u * step] = x;
         }
         dst += B * step;
@@ -199,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(const __grid_constant__ T
 // Row pass: forward rows of a (and b), pointwise product, inverse rows, inverse
 // four-step twiddle with the 2^32 / T scale. grid = (R, np); writes over a's rows.
 template <class A, bool SQUARE, int LOG_C>
-__global__ void __launch_bounds__(kRowThreads) k_rows(const __grid_constant__ TransformArgs g) {
+__global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     constexpr int C = 1 << LOG_C;
     constexpr int VS = padded_len(C);
@@ -212,6 +233,16 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(const __grid_constant__ Tr
         m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C));
     u32* sa = sm;
     u32* sb = sm + VS;
+    // This row's inverse four-step factors: 64 low-digit entries, then C / 64 high.
+    uint2* il = reinterpret_cast<uint2*>(sm + (SQUARE ? 1 : 2) * VS);
+    uint2* ih = il + (1 << kRowTwLoBits);
+    {
+        const uint2* lo = pp.i4_lo + ((size_t)row << kRowTwLoBits);
+        const uint2* hi = pp.i4_hi + ((size_t)row << (LOG_C - kRowTwLoBits));
+        constexpr int NL = 1 << kRowTwLoBits;
+        for (int i = threadIdx.x; i < NL + (C >> kRowTwLoBits); i += kRowThreads)
+            il[i] = __ldg(i < NL ? lo + i : hi + (i - NL));
+    }
 #pragma unroll 4
     for (int q = threadIdx.x; q < (C >> 2); q += kRowThreads) {
         const int k = pad_index(q << 2);
@@ -231,25 +262,24 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(const __grid_constant__ Tr
     }
     __syncthreads();
     dit_full<A, LOG_C, kRowThreads>(sa, 1, VS, pp.inv, pp.p);
-    const u32 rowexp = __brev((u32)row) >> (32 - g.log_r);
-    const u32 lo_mask = (1u << g.s_bits) - 1;
+    // Inverse four-step twiddle of n2 = 4q + t: i4_lo of lo = 4 (q mod 16) + t,
+    // i4_hi of hi = q / 16 (the scale is folded into the latter).
+    static_assert(kRowTwLoBits == 6, "four elements per thread, 16 groups per low digit");
 #pragma unroll 4
     for (int q = threadIdx.x; q < (C >> 2); q += kRowThreads) {
         const int k = pad_index(q << 2);
+        const uint2 h = ih[q >> 4];
+        const uint2* lq = il + (q & 15);
         u32 v[4];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const u32 ex = (u32)((q << 2) + t) * rowexp;
-            const u32 x = A::mulc(sa[k + t], __ldg(pp.i4_lo + (ex & lo_mask)), pp.p);
-            v[t] = A::mulc(x, __ldg(pp.i4_hi + (ex >> g.s_bits)), pp.p);
-        }
+        for (int t = 0; t < 4; ++t) v[t] = A::mulc(A::mulc(sa[k + t], lq[16 * t], pp.p), h, pp.p);
         ra[q] = make_uint4(v[0], v[1], v[2], v[3]);
     }
 }
 
 // Column pass of the inverse four-step: column DIT, canonical residues in place.
 template <class A, int LOG_R>
-__global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ TransformArgs g) {
+__global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     using M = ColumnMap<LOG_R>;
     constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;
@@ -294,10 +324,20 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(const __grid_constant__ T
 
 constexpr int kSmemOptIn = 200 * 1024;
 
-// Column residues plus the level root table (8-byte entries, 16-byte aligned).
-static size_t col_smem(int log_r) {
-    const size_t words = (size_t)col_vstride(log_r) * (1 << col_group_log(log_r));
-    return ((words * sizeof(u32) + 15) & ~(size_t)15) + ((size_t)8 << log_r);
+// Column residues plus the level root table (8-byte entries, 16-byte aligned); the
+// forward pass adds its per-sweep four-step factors (G rows of SW + 1 entries).
+static size_t col_smem(int log_r, bool fwd) {
+    const int log_g = col_group_log(log_r);
+    const size_t words = (size_t)col_vstride(log_r) * (1 << log_g);
+    const size_t sweeps = (size_t)1 << (log_r - kColLogRS);
+    return ((words * sizeof(u32) + 15) & ~(size_t)15) + ((size_t)8 << log_r) +
+           (fwd ? 8 * ((size_t)1 << log_g) * (sweeps + 1) : 0);
+}
+
+// Row residues (one or two vectors) plus the row's inverse four-step factors.
+static size_t row_smem(int log_c, bool square) {
+    return (size_t)(square ? 1 : 2) * padded_len(1 << log_c) * sizeof(u32) +
+           8 * (((size_t)1 << kRowTwLoBits) + ((size_t)1 << (log_c - kRowTwLoBits)));
 }
 
 // Preferred shared-memory carveout (percent of the unified L1/shared capacity) of
@@ -333,7 +373,7 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
     if (init) return opt_in(k, NTT_COLS_CARVEOUT);
     const unsigned ops = g.op_count ? g.op_count : (square ? 1 : 2);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : ops);
-    const size_t smem = col_smem(L);
+    const size_t smem = col_smem(L, true);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
@@ -343,7 +383,7 @@ static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st,
     auto k = square ? k_rows<A, true, L> : k_rows<A, false, L>;
     if (init) return opt_in(k, NTT_ROWS_CARVEOUT);
     const dim3 grid(1u << g.log_r, g.np, g.batch ? g.count : 1);
-    const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
+    const size_t smem = row_smem(L, square);
     k<<<grid, kRowThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
@@ -353,7 +393,7 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
     auto k = k_inv_cols<A, L>;
     if (init) return opt_in(k, NTT_COLS_CARVEOUT);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? g.count : 1);
-    const size_t smem = col_smem(L);
+    const size_t smem = col_smem(L, false);
     k<<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
