@@ -32,25 +32,35 @@ __device__ __forceinline__ constexpr int slot_offset(int m) {
     return m * S + ((m * S) >> 5);
 }
 
-template <class A, int LOG_N, int LEVEL, int RB, int NT>
-__device__ __forceinline__ void dif_pass(u32* __restrict__ s, int nvec, int vstride, const uint2* __restrict__ tw,
-                                         u32 p) {
+// Vectors a thread transforms together: register blocks at the same position of
+// two vectors share their twiddles, so each twiddle load serves both and the two
+// butterfly chains interleave.
+template <int NV>
+__host__ __device__ constexpr int vectors_per_block() { return NV % 2 == 0 ? 2 : 1; }
+
+// One pass of RB forward levels starting at LEVEL over NV vectors of 2^LOG_N points,
+// VS words apart.
+template <class A, int LOG_N, int LEVEL, int RB, int NT, int NV, int VS>
+__device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __restrict__ tw, u32 p) {
     constexpr int E = 1 << RB;
     constexpr int LOG_HQ = LOG_N - LEVEL - RB;
     constexpr int HQ = 1 << LOG_HQ;
     constexpr int LOG_GPV = LOG_N - RB;
-    const int total = nvec << LOG_GPV;
+    constexpr int VP = vectors_per_block<NV>();
+    constexpr int ITEMS = (NV / VP) << LOG_GPV;
 #pragma unroll 1
-    for (int g = threadIdx.x; g < total; g += NT) {
-        const int v = g >> LOG_GPV;
-        const int gg = g & ((1 << LOG_GPV) - 1);
+    for (int it = threadIdx.x; it < ITEMS; it += NT) {
+        const int v = (it >> LOG_GPV) * VP;
+        const int gg = it & ((1 << LOG_GPV) - 1);
         const int j0 = gg & (HQ - 1);
         const int i0 = ((gg >> LOG_HQ) << (LOG_HQ + RB)) + j0;
-        u32* base = s + v * vstride + pad_index(i0);
+        u32* base = s + v * VS + pad_index(i0);
         const uint2* twb = tw + j0;
-        u32 x[E];
+        u32 x[VP][E];
 #pragma unroll
-        for (int m = 0; m < E; ++m) x[m] = base[slot_offset<HQ>(m)];
+        for (int q = 0; q < VP; ++q)
+#pragma unroll
+            for (int m = 0; m < E; ++m) x[q][m] = base[q * VS + slot_offset<HQ>(m)];
 #pragma unroll
         for (int t = 0; t < RB; ++t) {
             const int half = E >> (t + 1);
@@ -59,32 +69,38 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, int nvec, int vstr
                 // butterflies (m, m + half) with m = blk*2*half + c share twiddle c
                 const uint2 w = twb[HQ * half + c * HQ];
 #pragma unroll
-                for (int b = 0; b < E; b += 2 * half) A::dif(x[b + c], x[b + c + half], w, p);
+                for (int q = 0; q < VP; ++q)
+#pragma unroll
+                    for (int b = 0; b < E; b += 2 * half) A::dif(x[q][b + c], x[q][b + c + half], w, p);
             }
         }
 #pragma unroll
-        for (int m = 0; m < E; ++m) base[slot_offset<HQ>(m)] = x[m];
+        for (int q = 0; q < VP; ++q)
+#pragma unroll
+            for (int m = 0; m < E; ++m) base[q * VS + slot_offset<HQ>(m)] = x[q][m];
     }
 }
 
-template <class A, int LOG_N, int LEVEL, int RB, int NT>
-__device__ __forceinline__ void dit_pass(u32* __restrict__ s, int nvec, int vstride, const uint2* __restrict__ tw,
-                                         u32 p) {
+template <class A, int LOG_N, int LEVEL, int RB, int NT, int NV, int VS>
+__device__ __forceinline__ void dit_pass(u32* __restrict__ s, const uint2* __restrict__ tw, u32 p) {
     constexpr int E = 1 << RB;
     constexpr int HS = 1 << LEVEL;
     constexpr int LOG_GPV = LOG_N - RB;
-    const int total = nvec << LOG_GPV;
+    constexpr int VP = vectors_per_block<NV>();
+    constexpr int ITEMS = (NV / VP) << LOG_GPV;
 #pragma unroll 1
-    for (int g = threadIdx.x; g < total; g += NT) {
-        const int v = g >> LOG_GPV;
-        const int gg = g & ((1 << LOG_GPV) - 1);
+    for (int it = threadIdx.x; it < ITEMS; it += NT) {
+        const int v = (it >> LOG_GPV) * VP;
+        const int gg = it & ((1 << LOG_GPV) - 1);
         const int j0 = gg & (HS - 1);
         const int i0 = ((gg >> LEVEL) << (LEVEL + RB)) + j0;
-        u32* base = s + v * vstride + pad_index(i0);
+        u32* base = s + v * VS + pad_index(i0);
         const uint2* twb = tw + j0;
-        u32 x[E];
+        u32 x[VP][E];
 #pragma unroll
-        for (int m = 0; m < E; ++m) x[m] = base[slot_offset<HS>(m)];
+        for (int q = 0; q < VP; ++q)
+#pragma unroll
+            for (int m = 0; m < E; ++m) x[q][m] = base[q * VS + slot_offset<HS>(m)];
 #pragma unroll
         for (int t = 0; t < RB; ++t) {
             const int dist = 1 << t;
@@ -92,11 +108,15 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, int nvec, int vstr
             for (int c = 0; c < dist; ++c) {
                 const uint2 w = twb[(HS << t) + c * HS];
 #pragma unroll
-                for (int b = 0; b < E; b += 2 * dist) A::dit(x[b + c], x[b + c + dist], w, p);
+                for (int q = 0; q < VP; ++q)
+#pragma unroll
+                    for (int b = 0; b < E; b += 2 * dist) A::dit(x[q][b + c], x[q][b + c + dist], w, p);
             }
         }
 #pragma unroll
-        for (int m = 0; m < E; ++m) base[slot_offset<HS>(m)] = x[m];
+        for (int q = 0; q < VP; ++q)
+#pragma unroll
+            for (int m = 0; m < E; ++m) base[q * VS + slot_offset<HS>(m)] = x[q][m];
     }
 }
 
@@ -106,32 +126,33 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, int nvec, int vstr
 #endif
 constexpr int kMaxRB = NTT_MAX_RB;
 
-// Full forward transform of nvec vectors of 2^LOG_N points; ends with a barrier.
-template <class A, int LOG_N, int NT, int LEVEL = 0>
-__device__ __forceinline__ void dif_full(u32* s, int nvec, int vstride, const uint2* tw, u32 p) {
+// Full forward transform of NV vectors of 2^LOG_N points, VS words apart; ends
+// with a barrier.
+template <class A, int LOG_N, int NT, int NV, int VS, int LEVEL = 0>
+__device__ __forceinline__ void dif_full(u32* s, const uint2* tw, u32 p) {
     if constexpr (LOG_N - LEVEL >= kMaxRB) {
-        dif_pass<A, LOG_N, LEVEL, kMaxRB, NT>(s, nvec, vstride, tw, p);
+        dif_pass<A, LOG_N, LEVEL, kMaxRB, NT, NV, VS>(s, tw, p);
         __syncthreads();
-        dif_full<A, LOG_N, NT, LEVEL + kMaxRB>(s, nvec, vstride, tw, p);
+        dif_full<A, LOG_N, NT, NV, VS, LEVEL + kMaxRB>(s, tw, p);
     } else if constexpr (LOG_N - LEVEL > 0) {
-        dif_pass<A, LOG_N, LEVEL, LOG_N - LEVEL, NT>(s, nvec, vstride, tw, p);
+        dif_pass<A, LOG_N, LEVEL, LOG_N - LEVEL, NT, NV, VS>(s, tw, p);
         __syncthreads();
     }
 }
 
 // Full inverse transform (unscaled); the short pass runs first. Ends with a barrier.
-template <class A, int LOG_N, int NT, int LEVEL = -1>
-__device__ __forceinline__ void dit_full(u32* s, int nvec, int vstride, const uint2* tw, u32 p) {
+template <class A, int LOG_N, int NT, int NV, int VS, int LEVEL = -1>
+__device__ __forceinline__ void dit_full(u32* s, const uint2* tw, u32 p) {
     if constexpr (LEVEL < 0) {
         constexpr int R0 = LOG_N % kMaxRB;
         if constexpr (R0 > 0) {
-            dit_pass<A, LOG_N, 0, R0, NT>(s, nvec, vstride, tw, p);
+            dit_pass<A, LOG_N, 0, R0, NT, NV, VS>(s, tw, p);
             __syncthreads();
         }
-        dit_full<A, LOG_N, NT, R0>(s, nvec, vstride, tw, p);
+        dit_full<A, LOG_N, NT, NV, VS, R0>(s, tw, p);
     } else if constexpr (LEVEL < LOG_N) {
-        dit_pass<A, LOG_N, LEVEL, kMaxRB, NT>(s, nvec, vstride, tw, p);
+        dit_pass<A, LOG_N, LEVEL, kMaxRB, NT, NV, VS>(s, tw, p);
         __syncthreads();
-        dit_full<A, LOG_N, NT, LEVEL + kMaxRB>(s, nvec, vstride, tw, p);
+        dit_full<A, LOG_N, NT, NV, VS, LEVEL + kMaxRB>(s, tw, p);
     }
 }

@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
         if (!m.square) sb[pad_index(i)] = (u64)i < m.lb ? reduce_coefficient<A, SIGNED>(__ldg(m.b + i), pp) : 0u;
     }
     __syncthreads();
-    dif_full<A, LOG_N, kThreads>(sm, m.square ? 1 : 2, VS, pp.fwd, pp.p);
+    if (m.square) dif_full<A, LOG_N, kThreads, 1, VS>(sm, pp.fwd, pp.p);
+    else dif_full<A, LOG_N, kThreads, 2, VS>(sm, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < N; i += kThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
         sa[k] = A::mulc(A::pointwise(x, y, pp.p, pp.pni), pp.scale, pp.p);
     }
     __syncthreads();
-    dit_full<A, LOG_N, kThreads>(sa, 1, VS, pp.inv, pp.p);
+    dit_full<A, LOG_N, kThreads, 1, VS>(sa, pp.inv, pp.p);
     u32* out = m.spec + ((size_t)blockIdx.x << LOG_N);
     for (int i = threadIdx.x; i < (int)m.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
 }
@@ -198,7 +199,7 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
         for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u] ? reduce_coefficient<A, SIGNED>(x[u], pp) : 0u;
     }
     __syncthreads();
-    dif_full<A, LOG_R, kThreads>(sm, M::G, M::VS, tw, pp.p);
+    dif_full<A, LOG_R, kThreads, M::G, M::VS>(sm, tw, pp.p);
     // Four-step twiddle w_T^(col * brev(row)) = fa * fb[col][brev(k)], then the store.
     u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
     const uint2* fbc = fb + M::col() * (M::SWEEPS + 1);
@@ -254,14 +255,15 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
         }
     }
     __syncthreads();
-    dif_full<A, LOG_C, kRowThreads>(sm, m.square ? 1 : 2, VS, pp.fwd, pp.p);
+    if (SQUARE || m.square) dif_full<A, LOG_C, kRowThreads, 1, VS>(sm, pp.fwd, pp.p);
+    else dif_full<A, LOG_C, kRowThreads, 2, VS>(sm, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < C; i += kRowThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
         sa[k] = A::pointwise(x, m.square ? x : sb[k], pp.p, pp.pni);
     }
     __syncthreads();
-    dit_full<A, LOG_C, kRowThreads>(sa, 1, VS, pp.inv, pp.p);
+    dit_full<A, LOG_C, kRowThreads, 1, VS>(sa, pp.inv, pp.p);
     // Inverse four-step twiddle of n2 = 4q + t: i4_lo of lo = 4 (q mod 16) + t,
     // i4_hi of hi = q / 16 (the scale is folded into the latter).
     static_assert(kRowTwLoBits == 6, "four elements per thread, 16 groups per low digit");
@@ -306,7 +308,7 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
         for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u];
     }
     __syncthreads();
-    dit_full<A, LOG_R, kThreads>(sm, M::G, M::VS, tw, pp.p);
+    dit_full<A, LOG_R, kThreads, M::G, M::VS>(sm, tw, pp.p);
     q = base;
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
