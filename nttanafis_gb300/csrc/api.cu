@@ -887,7 +887,7 @@ int ntt_timing_stop(float* ms, int capacity) {
 
 // ---------------------------------------------------------------------------------
 // Batches: many products and convolutions in one enqueue. Members are grouped by
-// transform class (kind, length, primes, sign); each class runs as one launch of
+// transform class (kind, length, primes, sign, square); each class runs as one launch of
 // every kernel of its path, with the member index in the last grid dimension.
 
 struct ntt_batch {
@@ -968,10 +968,10 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         if (!cuda_ok(cudaMemsetAsync(reqs[i].dst, 0, ((size_t)reqs[i].a_len + reqs[i].b_len) * 8, st), "zero product"))
             return 0;
     if (members.empty()) return 1;
-    // Group by class: kind, schoolbook, transform length, primes, sign.
+    // Group by class: kind, schoolbook, transform length, primes, sign, square.
     std::sort(members.begin(), members.end(), [](const Member& x, const Member& y) {
-        return std::make_tuple(x.g.conv, x.g.schoolbook, x.g.log_t, x.g.np, x.g.sign, x.index) <
-               std::make_tuple(y.g.conv, y.g.schoolbook, y.g.log_t, y.g.np, y.g.sign, y.index);
+        return std::make_tuple(x.g.conv, x.g.schoolbook, x.g.log_t, x.g.np, x.g.sign, x.square, x.index) <
+               std::make_tuple(y.g.conv, y.g.schoolbook, y.g.log_t, y.g.np, y.g.sign, y.square, y.index);
     });
     if (!b->arena.ensure(std::max<u64>(arena_bytes, 256)) || !b->desc.ensure(members.size() * sizeof(ProductDesc)))
         return 0;
@@ -1017,8 +1017,10 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         size_t end = k + 1;
         while (end < members.size() && end - k < kMaxLaunchMembers && members[end].g.conv == g0.conv &&
                members[end].g.schoolbook == g0.schoolbook && members[end].g.log_t == g0.log_t &&
-               members[end].g.np == g0.np && members[end].g.sign == g0.sign)
+               members[end].g.np == g0.np && members[end].g.sign == g0.sign &&
+               members[end].square == members[k].square)
             ++end;
+        const bool sq = members[k].square;
         const int n = (int)(end - k);
         if (g0.conv && g0.schoolbook) {
             for (size_t i = k; i < end; ++i) {
@@ -1043,13 +1045,13 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         const bool sign = g0.sign != 0;
         if (g0.log_t <= kMaxBlockLog) {
             g_launches += 1;
-            if (!cuda_ok(launch_small(ta, false, sign, st), "batched transform launch")) return 0;
+            if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return 0;
         } else {
             ta.log_r = g0.log_t / 2;
             ta.log_c = g0.log_t - ta.log_r;
             g_launches += 3;
-            if (!cuda_ok(launch_fwd_cols(ta, false, sign, st), "batched column pass launch") ||
-                !cuda_ok(launch_rows(ta, false, st), "batched row pass launch") ||
+            if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch") ||
+                !cuda_ok(launch_rows(ta, sq, st), "batched row pass launch") ||
                 !cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch"))
                 return 0;
         }

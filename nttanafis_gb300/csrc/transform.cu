@@ -104,15 +104,14 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     u32* sb = sm + VS;
     for (int i = threadIdx.x; i < N; i += kThreads) {
         sa[pad_index(i)] = (u64)i < m.la ? reduce_coefficient<A, SIGNED>(__ldg(m.a + i), pp) : 0u;
-        if (!m.square) sb[pad_index(i)] = (u64)i < m.lb ? reduce_coefficient<A, SIGNED>(__ldg(m.b + i), pp) : 0u;
+        if (!SQUARE) sb[pad_index(i)] = (u64)i < m.lb ? reduce_coefficient<A, SIGNED>(__ldg(m.b + i), pp) : 0u;
     }
     __syncthreads();
-    if (m.square) dif_full<A, LOG_N, kThreads, 1, VS>(sm, pp.fwd, pp.p);
-    else dif_full<A, LOG_N, kThreads, 2, VS>(sm, pp.fwd, pp.p);
+    dif_full<A, LOG_N, kThreads, SQUARE ? 1 : 2, VS>(sm, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < N; i += kThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
-        const u32 y = m.square ? x : sb[k];
+        const u32 y = SQUARE ? x : sb[k];
         sa[k] = A::mulc(A::pointwise(x, y, pp.p, pp.pni), pp.scale, pp.p);
     }
     __syncthreads();
@@ -249,18 +248,17 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
         const int k = pad_index(q << 2);
         const uint4 v = __ldcs(ra + q);
         sa[k] = v.x; sa[k + 1] = v.y; sa[k + 2] = v.z; sa[k + 3] = v.w;
-        if (!m.square) {
+        if (!SQUARE) {
             const uint4 w = __ldcs(rb + q);
             sb[k] = w.x; sb[k + 1] = w.y; sb[k + 2] = w.z; sb[k + 3] = w.w;
         }
     }
     __syncthreads();
-    if (SQUARE || m.square) dif_full<A, LOG_C, kRowThreads, 1, VS>(sm, pp.fwd, pp.p);
-    else dif_full<A, LOG_C, kRowThreads, 2, VS>(sm, pp.fwd, pp.p);
+    dif_full<A, LOG_C, kRowThreads, SQUARE ? 1 : 2, VS>(sm, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < C; i += kRowThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
-        sa[k] = A::pointwise(x, m.square ? x : sb[k], pp.p, pp.pni);
+        sa[k] = A::pointwise(x, SQUARE ? x : sb[k], pp.p, pp.pni);
     }
     __syncthreads();
     dit_full<A, LOG_C, kRowThreads, 1, VS>(sa, pp.inv, pp.p);
