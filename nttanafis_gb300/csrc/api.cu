@@ -349,7 +349,7 @@ static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
             const u32 c = powmod(iw, bit_reverse((u32)row, log_r), p);  // w^-k1
             u32 x = 1;
             for (u64 lo = 0; lo < NL; ++lo, x = mulmod(x, c, p))
-                ilo[row * NL + 16 * (lo & 3) + (lo >> 2)] = shoup_pair(x, p);
+                ilo[row * NL + lo] = shoup_pair(x, p);
             const u32 c64 = x;  // w^(-k1 * 64)
             x = scale;
             for (u64 hi = 0; hi < NH; ++hi, x = mulmod(x, c64, p)) ihi[row * NH + hi] = shoup_pair(x, p);

@@ -33,8 +33,7 @@ constexpr int kColLogRS = 8 - kColLogG;
 //    f4_b[col * SW + brev(k)] = w_T^(col * brev(k)) (one per sweep);
 //  - inverse, applied by the row pass: w_T^(-k1 * n2) times the inverse scale for
 //    the row of frequency k1 = brev(row) and n2 = 64 * hi + lo, as
-//    i4_lo[row * 64 + 16 * (lo mod 4) + lo / 4] = w_T^(-k1 * lo) (ordered so that a
-//    warp's reads of consecutive 4-element groups hit consecutive words) times
+//    i4_lo[row * 64 + lo] = w_T^(-k1 * lo) times
 //    i4_hi[row * C / 64 + hi] = w_T^(-k1 * 64 * hi) * scale.
 constexpr int kRowTwLoBits = 6;
 

@@ -38,8 +38,48 @@ __device__ __forceinline__ constexpr int slot_offset(int m) {
 template <int NV>
 __host__ __device__ constexpr int vectors_per_block() { return NV % 2 == 0 ? 2 : 1; }
 
+// RB forward levels on VP register blocks of 2^RB points spaced H apart; the
+// twiddle of butterfly c at the level of half-size h = 2^(RB-1-t) * H is
+// twb[h + c * H], twb = table + (first point mod H).
+template <class A, int RB, int H, int VP>
+__device__ __forceinline__ void dif_levels(u32 (&x)[VP][1 << RB], const uint2* __restrict__ twb, u32 p) {
+    constexpr int E = 1 << RB;
+#pragma unroll
+    for (int t = 0; t < RB; ++t) {
+        const int half = E >> (t + 1);
+#pragma unroll
+        for (int c = 0; c < half; ++c) {
+            // butterflies (m, m + half) with m = blk*2*half + c share twiddle c
+            const uint2 w = twb[H * half + c * H];
+#pragma unroll
+            for (int q = 0; q < VP; ++q)
+#pragma unroll
+                for (int b = 0; b < E; b += 2 * half) A::dif(x[q][b + c], x[q][b + c + half], w, p);
+        }
+    }
+}
+
+// RB inverse levels on VP register blocks of 2^RB points spaced H apart.
+template <class A, int RB, int H, int VP>
+__device__ __forceinline__ void dit_levels(u32 (&x)[VP][1 << RB], const uint2* __restrict__ twb, u32 p) {
+    constexpr int E = 1 << RB;
+#pragma unroll
+    for (int t = 0; t < RB; ++t) {
+        const int dist = 1 << t;
+#pragma unroll
+        for (int c = 0; c < dist; ++c) {
+            const uint2 w = twb[(H << t) + c * H];
+#pragma unroll
+            for (int q = 0; q < VP; ++q)
+#pragma unroll
+                for (int b = 0; b < E; b += 2 * dist) A::dit(x[q][b + c], x[q][b + c + dist], w, p);
+        }
+    }
+}
+
 // One pass of RB forward levels starting at LEVEL over NV vectors of 2^LOG_N points,
-// VS words apart.
+// VS words apart. Register block gg of a vector starts at point
+// i0 = (gg / HQ) * HQ * 2^RB + gg mod HQ and spans 2^RB points HQ apart.
 template <class A, int LOG_N, int LEVEL, int RB, int NT, int NV, int VS>
 __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __restrict__ tw, u32 p) {
     constexpr int E = 1 << RB;
@@ -55,25 +95,12 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __res
         const int j0 = gg & (HQ - 1);
         const int i0 = ((gg >> LOG_HQ) << (LOG_HQ + RB)) + j0;
         u32* base = s + v * VS + pad_index(i0);
-        const uint2* twb = tw + j0;
         u32 x[VP][E];
 #pragma unroll
         for (int q = 0; q < VP; ++q)
 #pragma unroll
             for (int m = 0; m < E; ++m) x[q][m] = base[q * VS + slot_offset<HQ>(m)];
-#pragma unroll
-        for (int t = 0; t < RB; ++t) {
-            const int half = E >> (t + 1);
-#pragma unroll
-            for (int c = 0; c < half; ++c) {
-                // butterflies (m, m + half) with m = blk*2*half + c share twiddle c
-                const uint2 w = twb[HQ * half + c * HQ];
-#pragma unroll
-                for (int q = 0; q < VP; ++q)
-#pragma unroll
-                    for (int b = 0; b < E; b += 2 * half) A::dif(x[q][b + c], x[q][b + c + half], w, p);
-            }
-        }
+        dif_levels<A, RB, HQ, VP>(x, tw + j0, p);
 #pragma unroll
         for (int q = 0; q < VP; ++q)
 #pragma unroll
@@ -81,6 +108,8 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __res
     }
 }
 
+// One pass of RB inverse levels starting at LEVEL; block gg starts at
+// i0 = (gg / HS) * HS * 2^RB + gg mod HS with HS = 2^LEVEL.
 template <class A, int LOG_N, int LEVEL, int RB, int NT, int NV, int VS>
 __device__ __forceinline__ void dit_pass(u32* __restrict__ s, const uint2* __restrict__ tw, u32 p) {
     constexpr int E = 1 << RB;
@@ -95,24 +124,12 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, const uint2* __res
         const int j0 = gg & (HS - 1);
         const int i0 = ((gg >> LEVEL) << (LEVEL + RB)) + j0;
         u32* base = s + v * VS + pad_index(i0);
-        const uint2* twb = tw + j0;
         u32 x[VP][E];
 #pragma unroll
         for (int q = 0; q < VP; ++q)
 #pragma unroll
             for (int m = 0; m < E; ++m) x[q][m] = base[q * VS + slot_offset<HS>(m)];
-#pragma unroll
-        for (int t = 0; t < RB; ++t) {
-            const int dist = 1 << t;
-#pragma unroll
-            for (int c = 0; c < dist; ++c) {
-                const uint2 w = twb[(HS << t) + c * HS];
-#pragma unroll
-                for (int q = 0; q < VP; ++q)
-#pragma unroll
-                    for (int b = 0; b < E; b += 2 * dist) A::dit(x[q][b + c], x[q][b + c + dist], w, p);
-            }
-        }
+        dit_levels<A, RB, HS, VP>(x, tw + j0, p);
 #pragma unroll
         for (int q = 0; q < VP; ++q)
 #pragma unroll
@@ -137,6 +154,28 @@ __device__ __forceinline__ void dif_full(u32* s, const uint2* tw, u32 p) {
     } else if constexpr (LOG_N - LEVEL > 0) {
         dif_pass<A, LOG_N, LEVEL, LOG_N - LEVEL, NT, NV, VS>(s, tw, p);
         __syncthreads();
+    }
+}
+
+// Forward passes of kMaxRB levels from LEVEL up to END (exclusive), each followed by
+// a barrier.
+template <class A, int LOG_N, int NT, int NV, int VS, int LEVEL, int END>
+__device__ __forceinline__ void dif_range(u32* s, const uint2* tw, u32 p) {
+    if constexpr (LEVEL < END) {
+        dif_pass<A, LOG_N, LEVEL, kMaxRB, NT, NV, VS>(s, tw, p);
+        __syncthreads();
+        dif_range<A, LOG_N, NT, NV, VS, LEVEL + kMaxRB, END>(s, tw, p);
+    }
+}
+
+// Inverse passes of kMaxRB levels from LEVEL up to END (exclusive), each followed by
+// a barrier.
+template <class A, int LOG_N, int NT, int NV, int VS, int LEVEL, int END>
+__device__ __forceinline__ void dit_range(u32* s, const uint2* tw, u32 p) {
+    if constexpr (LEVEL < END) {
+        dit_pass<A, LOG_N, LEVEL, kMaxRB, NT, NV, VS>(s, tw, p);
+        __syncthreads();
+        dit_range<A, LOG_N, NT, NV, VS, LEVEL + kMaxRB, END>(s, tw, p);
     }
 }
 

@@ -219,22 +219,30 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
 
 // Row pass: forward rows of a (and b), pointwise product, inverse rows, inverse
 // four-step twiddle with the 2^32 / T scale. grid = (R, np); writes over a's rows.
+//
+// Shared memory is touched as little as the register blocks allow: the first
+// forward pass reads the rows from global memory, the last forward pass, the
+// pointwise product and the first inverse pass run on the same registers (both
+// work on blocks of 2^RBL consecutive points), and the last inverse pass applies
+// the twiddle and writes global memory.
 template <class A, bool SQUARE, int LOG_C>
 __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     constexpr int C = 1 << LOG_C;
     constexpr int VS = padded_len(C);
+    constexpr int NV = SQUARE ? 1 : 2;           // a (and b), transformed together
+    constexpr int RB = kMaxRB;
+    constexpr int RBL = LOG_C % RB ? LOG_C % RB : RB;  // levels of the fused middle pass
+    constexpr int LL = LOG_C - RBL;              // its first forward level
+    static_assert(LOG_C > RB, "at least two passes each way");
     const int prime = blockIdx.y;
     const int row = blockIdx.x;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, SQUARE);
-    uint4* ra = reinterpret_cast<uint4*>(m.spec + ((size_t)prime << g.log_t) + ((size_t)row << LOG_C));
-    const uint4* rb = reinterpret_cast<const uint4*>(
-        m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C));
-    u32* sa = sm;
-    u32* sb = sm + VS;
+    u32* ra = m.spec + ((size_t)prime << g.log_t) + ((size_t)row << LOG_C);
+    const u32* rb = m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C);
     // This row's inverse four-step factors: 64 low-digit entries, then C / 64 high.
-    uint2* il = reinterpret_cast<uint2*>(sm + (SQUARE ? 1 : 2) * VS);
+    uint2* il = reinterpret_cast<uint2*>(sm + NV * VS);
     uint2* ih = il + (1 << kRowTwLoBits);
     {
         const uint2* lo = pp.i4_lo + ((size_t)row << kRowTwLoBits);
@@ -243,37 +251,68 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
         for (int i = threadIdx.x; i < NL + (C >> kRowTwLoBits); i += kRowThreads)
             il[i] = __ldg(i < NL ? lo + i : hi + (i - NL));
     }
-#pragma unroll 4
-    for (int q = threadIdx.x; q < (C >> 2); q += kRowThreads) {
-        const int k = pad_index(q << 2);
-        const uint4 v = __ldcs(ra + q);
-        sa[k] = v.x; sa[k + 1] = v.y; sa[k + 2] = v.z; sa[k + 3] = v.w;
-        if (!SQUARE) {
-            const uint4 w = __ldcs(rb + q);
-            sb[k] = w.x; sb[k + 1] = w.y; sb[k + 2] = w.z; sb[k + 3] = w.w;
+    // First forward pass: global -> shared. Block gg holds points gg + k * HQ.
+    {
+        constexpr int HQ = C >> RB;
+#pragma unroll 1
+        for (int gg = threadIdx.x; gg < HQ; gg += kRowThreads) {
+            u32 x[NV][1 << RB];
+#pragma unroll
+            for (int k = 0; k < (1 << RB); ++k) {
+                x[0][k] = __ldcs(ra + gg + k * HQ);
+                if constexpr (NV == 2) x[NV - 1][k] = __ldcs(rb + gg + k * HQ);
+            }
+            dif_levels<A, RB, HQ, NV>(x, pp.fwd + gg, pp.p);
+            u32* base = sm + pad_index(gg);
+#pragma unroll
+            for (int q = 0; q < NV; ++q)
+#pragma unroll
+                for (int k = 0; k < (1 << RB); ++k) base[q * VS + slot_offset<HQ>(k)] = x[q][k];
         }
     }
     __syncthreads();
-    dif_full<A, LOG_C, kRowThreads, SQUARE ? 1 : 2, VS>(sm, pp.fwd, pp.p);
-    for (int i = threadIdx.x; i < C; i += kRowThreads) {
-        const int k = pad_index(i);
-        const u32 x = sa[k];
-        sa[k] = A::pointwise(x, SQUARE ? x : sb[k], pp.p, pp.pni);
+    dif_range<A, LOG_C, kRowThreads, NV, VS, RB, LL>(sm, pp.fwd, pp.p);
+    // Last forward pass, pointwise product, first inverse pass: blocks of 2^RBL
+    // consecutive points (twiddles of half-size below 2^RBL, shared by all blocks).
+    {
+        constexpr int E = 1 << RBL;
+#pragma unroll 1
+        for (int gg = threadIdx.x; gg < (C >> RBL); gg += kRowThreads) {
+            u32* base = sm + pad_index(gg << RBL);
+            u32 x[NV][E];
+#pragma unroll
+            for (int q = 0; q < NV; ++q)
+#pragma unroll
+                for (int k = 0; k < E; ++k) x[q][k] = base[q * VS + k];
+            dif_levels<A, RBL, 1, NV>(x, pp.fwd, pp.p);
+#pragma unroll
+            for (int k = 0; k < E; ++k) x[0][k] = A::pointwise(x[0][k], x[NV - 1][k], pp.p, pp.pni);
+            u32(&y)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
+            dit_levels<A, RBL, 1, 1>(y, pp.inv, pp.p);
+#pragma unroll
+            for (int k = 0; k < E; ++k) base[k] = x[0][k];
+        }
     }
     __syncthreads();
-    dit_full<A, LOG_C, kRowThreads, 1, VS>(sa, pp.inv, pp.p);
-    // Inverse four-step twiddle of n2 = 4q + t: i4_lo of lo = 4 (q mod 16) + t,
-    // i4_hi of hi = q / 16 (the scale is folded into the latter).
-    static_assert(kRowTwLoBits == 6, "four elements per thread, 16 groups per low digit");
-#pragma unroll 4
-    for (int q = threadIdx.x; q < (C >> 2); q += kRowThreads) {
-        const int k = pad_index(q << 2);
-        const uint2 h = ih[q >> 4];
-        const uint2* lq = il + (q & 15);
-        u32 v[4];
+    dit_range<A, LOG_C, kRowThreads, 1, VS, RBL, LOG_C - RB>(sm, pp.inv, pp.p);
+    // Last inverse pass: shared -> global, times the inverse four-step twiddle of
+    // n2 = 64 hi + lo (i4_lo of lo, i4_hi of hi with the scale folded in).
+    {
+        constexpr int HS = C >> RB;
+#pragma unroll 1
+        for (int gg = threadIdx.x; gg < HS; gg += kRowThreads) {
+            const u32* base = sm + pad_index(gg);
+            u32 x[1][1 << RB];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) v[t] = A::mulc(A::mulc(sa[k + t], lq[16 * t], pp.p), h, pp.p);
-        ra[q] = make_uint4(v[0], v[1], v[2], v[3]);
+            for (int k = 0; k < (1 << RB); ++k) x[0][k] = base[slot_offset<HS>(k)];
+            dit_levels<A, RB, HS, 1>(x, pp.inv + gg, pp.p);
+#pragma unroll
+            for (int k = 0; k < (1 << RB); ++k) {
+                const int n2 = gg + k * HS;
+                const uint2 lo = il[n2 & ((1 << kRowTwLoBits) - 1)];
+                ra[n2] = A::mulc(A::mulc(x[0][k], lo, pp.p), ih[n2 >> kRowTwLoBits], pp.p);
+            }
+        }
     }
 }
 
