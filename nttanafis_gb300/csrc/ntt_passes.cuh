@@ -21,6 +21,9 @@
 // Shared-memory slot of logical index i: one pad word per 32 words.
 __host__ __device__ constexpr int pad_index(int i) { return i + (i >> 5); }
 
+// log2 of a power of two.
+__host__ __device__ constexpr int ilog2(int n) { return n > 1 ? 1 + ilog2(n >> 1) : 0; }
+
 // Padded words that hold one vector of n points.
 __host__ __device__ constexpr int padded_len(int n) { return n + (n >> 5); }
 
@@ -34,9 +37,12 @@ __device__ __forceinline__ constexpr int slot_offset(int m) {
 
 // Vectors a thread transforms together: register blocks at the same position of
 // two vectors share their twiddles, so each twiddle load serves both and the two
-// butterfly chains interleave.
-template <int NV>
-__host__ __device__ constexpr int vectors_per_block() { return NV % 2 == 0 ? 2 : 1; }
+// butterfly chains interleave. Pairs are taken only while every thread still gets
+// a block (2^LOG_GPV blocks per vector, NT threads).
+template <int NV, int LOG_GPV, int NT>
+__host__ __device__ constexpr int vectors_per_block() {
+    return NV % 2 == 0 && ((NV / 2) << LOG_GPV) >= NT ? 2 : 1;
+}
 
 // RB forward levels on VP register blocks of 2^RB points spaced H apart; the
 // twiddle of butterfly c at the level of half-size h = 2^(RB-1-t) * H is
@@ -86,7 +92,7 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __res
     constexpr int LOG_HQ = LOG_N - LEVEL - RB;
     constexpr int HQ = 1 << LOG_HQ;
     constexpr int LOG_GPV = LOG_N - RB;
-    constexpr int VP = vectors_per_block<NV>();
+    constexpr int VP = vectors_per_block<NV, LOG_GPV, NT>();
     constexpr int ITEMS = (NV / VP) << LOG_GPV;
 #pragma unroll 1
     for (int it = threadIdx.x; it < ITEMS; it += NT) {
@@ -115,7 +121,7 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, const uint2* __res
     constexpr int E = 1 << RB;
     constexpr int HS = 1 << LEVEL;
     constexpr int LOG_GPV = LOG_N - RB;
-    constexpr int VP = vectors_per_block<NV>();
+    constexpr int VP = vectors_per_block<NV, LOG_GPV, NT>();
     constexpr int ITEMS = (NV / VP) << LOG_GPV;
 #pragma unroll 1
     for (int it = threadIdx.x; it < ITEMS; it += NT) {

@@ -217,8 +217,15 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     }
 }
 
+// Rows per CTA of the row pass: enough that every thread owns a register block of
+// the first pass (2^(log_c - kMaxRB) blocks per row).
+__host__ __device__ constexpr int row_log_rpc(int log_c) {
+    return log_c - kMaxRB >= ilog2(kRowThreads) ? 0 : ilog2(kRowThreads) - (log_c - kMaxRB);
+}
+
 // Row pass: forward rows of a (and b), pointwise product, inverse rows, inverse
-// four-step twiddle with the 2^32 / T scale. grid = (R, np); writes over a's rows.
+// four-step twiddle with the 2^32 / T scale. grid = (R / RPC, np); writes over a's
+// rows. A CTA owns RPC consecutive rows; shared memory holds vectors [RPC][a, b].
 //
 // Shared memory is touched as little as the register blocks allow: the first
 // forward pass reads the rows from global memory, the last forward pass, the
@@ -231,39 +238,44 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
     constexpr int C = 1 << LOG_C;
     constexpr int VS = padded_len(C);
     constexpr int NV = SQUARE ? 1 : 2;           // a (and b), transformed together
+    constexpr int LOG_RPC = row_log_rpc(LOG_C);
+    constexpr int RPC = 1 << LOG_RPC;
     constexpr int RB = kMaxRB;
     constexpr int RBL = LOG_C % RB ? LOG_C % RB : RB;  // levels of the fused middle pass
     constexpr int LL = LOG_C - RBL;              // its first forward level
-    static_assert(LOG_C > RB, "at least two passes each way");
+    constexpr int NL = 1 << kRowTwLoBits, NH = C >> kRowTwLoBits;
+    static_assert(LOG_C > RB && LOG_C > kRowTwLoBits, "at least two passes each way");
     const int prime = blockIdx.y;
-    const int row = blockIdx.x;
+    const int row0 = blockIdx.x << LOG_RPC;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, SQUARE);
-    u32* ra = m.spec + ((size_t)prime << g.log_t) + ((size_t)row << LOG_C);
-    const u32* rb = m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row << LOG_C);
-    // This row's inverse four-step factors: 64 low-digit entries, then C / 64 high.
-    uint2* il = reinterpret_cast<uint2*>(sm + NV * VS);
-    uint2* ih = il + (1 << kRowTwLoBits);
+    u32* ra = m.spec + ((size_t)prime << g.log_t) + ((size_t)row0 << LOG_C);
+    const u32* rb = m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row0 << LOG_C);
+    // The rows' inverse four-step factors: RPC x 64 low-digit entries, RPC x C/64 high.
+    uint2* il = reinterpret_cast<uint2*>(sm + RPC * NV * VS);
+    uint2* ih = il + RPC * NL;
     {
-        const uint2* lo = pp.i4_lo + ((size_t)row << kRowTwLoBits);
-        const uint2* hi = pp.i4_hi + ((size_t)row << (LOG_C - kRowTwLoBits));
-        constexpr int NL = 1 << kRowTwLoBits;
-        for (int i = threadIdx.x; i < NL + (C >> kRowTwLoBits); i += kRowThreads)
-            il[i] = __ldg(i < NL ? lo + i : hi + (i - NL));
+        const uint2* lo = pp.i4_lo + (size_t)row0 * NL;
+        const uint2* hi = pp.i4_hi + (size_t)row0 * NH;
+        for (int i = threadIdx.x; i < RPC * (NL + NH); i += kRowThreads)
+            il[i] = __ldg(i < RPC * NL ? lo + i : hi + (i - RPC * NL));
     }
-    // First forward pass: global -> shared. Block gg holds points gg + k * HQ.
+    // First forward pass: global -> shared. Block gg of a row holds points gg + k * HQ.
     {
-        constexpr int HQ = C >> RB;
+        constexpr int LOG_HQ = LOG_C - RB;
+        constexpr int HQ = 1 << LOG_HQ;
 #pragma unroll 1
-        for (int gg = threadIdx.x; gg < HQ; gg += kRowThreads) {
+        for (int it = threadIdx.x; it < (RPC << LOG_HQ); it += kRowThreads) {
+            const int r = it >> LOG_HQ, gg = it & (HQ - 1);
+            const size_t off = ((size_t)r << LOG_C) + gg;
             u32 x[NV][1 << RB];
 #pragma unroll
             for (int k = 0; k < (1 << RB); ++k) {
-                x[0][k] = __ldcs(ra + gg + k * HQ);
-                if constexpr (NV == 2) x[NV - 1][k] = __ldcs(rb + gg + k * HQ);
+                x[0][k] = __ldcs(ra + off + k * HQ);
+                if constexpr (NV == 2) x[NV - 1][k] = __ldcs(rb + off + k * HQ);
             }
             dif_levels<A, RB, HQ, NV>(x, pp.fwd + gg, pp.p);
-            u32* base = sm + pad_index(gg);
+            u32* base = sm + r * NV * VS + pad_index(gg);
 #pragma unroll
             for (int q = 0; q < NV; ++q)
 #pragma unroll
@@ -271,14 +283,15 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
         }
     }
     __syncthreads();
-    dif_range<A, LOG_C, kRowThreads, NV, VS, RB, LL>(sm, pp.fwd, pp.p);
+    dif_range<A, LOG_C, kRowThreads, RPC * NV, VS, RB, LL>(sm, pp.fwd, pp.p);
     // Last forward pass, pointwise product, first inverse pass: blocks of 2^RBL
     // consecutive points (twiddles of half-size below 2^RBL, shared by all blocks).
     {
         constexpr int E = 1 << RBL;
 #pragma unroll 1
-        for (int gg = threadIdx.x; gg < (C >> RBL); gg += kRowThreads) {
-            u32* base = sm + pad_index(gg << RBL);
+        for (int it = threadIdx.x; it < (RPC << (LOG_C - RBL)); it += kRowThreads) {
+            const int r = it >> (LOG_C - RBL), gg = it & ((C >> RBL) - 1);
+            u32* base = sm + r * NV * VS + pad_index(gg << RBL);
             u32 x[NV][E];
 #pragma unroll
             for (int q = 0; q < NV; ++q)
@@ -294,23 +307,27 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
         }
     }
     __syncthreads();
-    dit_range<A, LOG_C, kRowThreads, 1, VS, RBL, LOG_C - RB>(sm, pp.inv, pp.p);
+    dit_range<A, LOG_C, kRowThreads, RPC, NV * VS, RBL, LOG_C - RB>(sm, pp.inv, pp.p);
     // Last inverse pass: shared -> global, times the inverse four-step twiddle of
     // n2 = 64 hi + lo (i4_lo of lo, i4_hi of hi with the scale folded in).
     {
-        constexpr int HS = C >> RB;
+        constexpr int LOG_HS = LOG_C - RB;
+        constexpr int HS = 1 << LOG_HS;
 #pragma unroll 1
-        for (int gg = threadIdx.x; gg < HS; gg += kRowThreads) {
-            const u32* base = sm + pad_index(gg);
+        for (int it = threadIdx.x; it < (RPC << LOG_HS); it += kRowThreads) {
+            const int r = it >> LOG_HS, gg = it & (HS - 1);
+            const u32* base = sm + r * NV * VS + pad_index(gg);
             u32 x[1][1 << RB];
 #pragma unroll
             for (int k = 0; k < (1 << RB); ++k) x[0][k] = base[slot_offset<HS>(k)];
             dit_levels<A, RB, HS, 1>(x, pp.inv + gg, pp.p);
+            const uint2* lo = il + r * NL;
+            const uint2* hi = ih + r * NH;
+            u32* out = ra + ((size_t)r << LOG_C);
 #pragma unroll
             for (int k = 0; k < (1 << RB); ++k) {
                 const int n2 = gg + k * HS;
-                const uint2 lo = il[n2 & ((1 << kRowTwLoBits) - 1)];
-                ra[n2] = A::mulc(A::mulc(x[0][k], lo, pp.p), ih[n2 >> kRowTwLoBits], pp.p);
+                out[n2] = A::mulc(A::mulc(x[0][k], lo[n2 & (NL - 1)], pp.p), hi[n2 >> kRowTwLoBits], pp.p);
             }
         }
     }
@@ -373,10 +390,11 @@ static size_t col_smem(int log_r, bool fwd) {
            (fwd ? 8 * ((size_t)1 << log_g) * (sweeps + 1) : 0);
 }
 
-// Row residues (one or two vectors) plus the row's inverse four-step factors.
+// Row residues (one or two vectors per row) plus the rows' inverse four-step factors.
 static size_t row_smem(int log_c, bool square) {
-    return (size_t)(square ? 1 : 2) * padded_len(1 << log_c) * sizeof(u32) +
-           8 * (((size_t)1 << kRowTwLoBits) + ((size_t)1 << (log_c - kRowTwLoBits)));
+    const size_t rpc = (size_t)1 << row_log_rpc(log_c);
+    return rpc * ((size_t)(square ? 1 : 2) * padded_len(1 << log_c) * sizeof(u32) +
+                  8 * (((size_t)1 << kRowTwLoBits) + ((size_t)1 << (log_c - kRowTwLoBits))));
 }
 
 // Preferred shared-memory carveout (percent of the unified L1/shared capacity) of
@@ -421,7 +439,7 @@ template <class A, int L>
 static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
     auto k = square ? k_rows<A, true, L> : k_rows<A, false, L>;
     if (init) return opt_in(k, NTT_ROWS_CARVEOUT);
-    const dim3 grid(1u << g.log_r, g.np, g.batch ? g.count : 1);
+    const dim3 grid(1u << (g.log_r - row_log_rpc(L)), g.np, g.batch ? g.count : 1);
     const size_t smem = row_smem(L, square);
     k<<<grid, kRowThreads, smem, st>>>(g);
     return cudaGetLastError();
