@@ -46,8 +46,9 @@ __host__ __device__ constexpr int vectors_per_block() {
 
 // RB forward levels on VP register blocks of 2^RB points spaced H apart; the
 // twiddle of butterfly c at the level of half-size h = 2^(RB-1-t) * H is
-// twb[h + c * H], twb = table + (first point mod H).
-template <class A, int RB, int H, int VP>
+// twb[h + c * H], twb = table + (first point mod H). With HZ the upper half of
+// every block is zero, so the first level only multiplies: (x, 0) -> (x, x*w).
+template <class A, int RB, int H, int VP, bool HZ = false>
 __device__ __forceinline__ void dif_levels(u32 (&x)[VP][1 << RB], const uint2* __restrict__ twb, u32 p) {
     constexpr int E = 1 << RB;
 #pragma unroll
@@ -60,7 +61,10 @@ __device__ __forceinline__ void dif_levels(u32 (&x)[VP][1 << RB], const uint2* _
 #pragma unroll
             for (int q = 0; q < VP; ++q)
 #pragma unroll
-                for (int b = 0; b < E; b += 2 * half) A::dif(x[q][b + c], x[q][b + c + half], w, p);
+                for (int b = 0; b < E; b += 2 * half) {
+                    if (HZ && t == 0) x[q][b + c + half] = A::mulc(x[q][b + c], w, p);
+                    else A::dif(x[q][b + c], x[q][b + c + half], w, p);
+                }
         }
     }
 }

@@ -168,13 +168,11 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
     const int log_c = g.log_c;
-    const u32 col = (u32)(blockIdx.x << M::LOG_G) + M::col();
+    const u32 col0 = (u32)(blockIdx.x << M::LOG_G);
+    const u32 col = col0 + M::col();
     const int r0 = M::row0();
-    // Sweeps k < live read coefficients; the rest are zero padding.
     const u64 first = ((u64)r0 << log_c) + col;
     const u64 step = (u64)M::RS << log_c;
-    const int live = first >= len ? 0 : (int)min((u64)M::SWEEPS, (len - first + step - 1) / step);
-    const u64* __restrict__ p = src + first;
     u32* s = sm + M::slot0();
     uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
     load_table<LOG_R>(tw, pp.fwd);
@@ -182,23 +180,48 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     // so that the G columns of a warp read distinct banks.
     uint2* fb = tw + (1 << LOG_R);
     {
-        const uint2* src = pp.f4_b + ((size_t)(blockIdx.x << M::LOG_G) << M::LOG_SW);
+        const uint2* src = pp.f4_b + ((size_t)col0 << M::LOG_SW);
         for (int i = threadIdx.x; i < (M::G << M::LOG_SW); i += kThreads)
             fb[(i >> M::LOG_SW) * (M::SWEEPS + 1) + (i & (M::SWEEPS - 1))] = __ldg(src + i);
     }
     const uint2 fa = __ldg(pp.f4_a + ((size_t)col << kColLogRS) + (__brev((u32)r0) >> (32 - kColLogRS)));
+    // First forward pass fused with the limb reduction (its roots come from global
+    // memory: the shared table is published by the barrier after it). Item it takes
+    // column c = it mod G and block gg = it / G (rows gg + k * HQ), so a warp loads
+    // four rows of G consecutive limbs at a time and stores to distinct banks. When
+    // len <= T/2 (every balanced product) rows R/2 and above hold no limb: their
+    // loads and the first level's butterflies are skipped.
+    {
+        constexpr int RB = kMaxRB, LOG_HQ = LOG_R - RB, HQ = 1 << LOG_HQ, E = 1 << RB;
+        const bool half = len <= ((u64)1 << (g.log_t - 1));
+        const u64 kstep = (u64)HQ << log_c;
 #pragma unroll 1
-    for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
-        u64 x[B];
+        for (int it = threadIdx.x; it < (M::G << LOG_HQ); it += kThreads) {
+            const int c = it & (M::G - 1), gg = it >> M::LOG_G;
+            const u64 n0 = ((u64)gg << log_c) + col0 + c;
+            u32 x[1][E];
+            if (half) {
 #pragma unroll
-        for (int u = 0; u < B; ++u) x[u] = (k0 + u < live) ? __ldcs(p + u * step) : 0ull;
-        p += B * step;
-        u32* sk = s + slot_offset<M::RS>(k0);
+                for (int k = 0; k < E / 2; ++k) {
+                    const u64 n = n0 + k * kstep;
+                    x[0][k] = n < len ? reduce_coefficient<A, SIGNED>(__ldcs(src + n), pp) : 0u;
+                }
+                dif_levels<A, RB, HQ, 1, true>(x, pp.fwd + gg, pp.p);
+            } else {
 #pragma unroll
-        for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u] ? reduce_coefficient<A, SIGNED>(x[u], pp) : 0u;
+                for (int k = 0; k < E; ++k) {
+                    const u64 n = n0 + k * kstep;
+                    x[0][k] = n < len ? reduce_coefficient<A, SIGNED>(__ldcs(src + n), pp) : 0u;
+                }
+                dif_levels<A, RB, HQ, 1>(x, pp.fwd + gg, pp.p);
+            }
+            u32* base = sm + c * M::VS + pad_index(gg);
+#pragma unroll
+            for (int k = 0; k < E; ++k) base[slot_offset<HQ>(k)] = x[0][k];
+        }
     }
     __syncthreads();
-    dif_full<A, LOG_R, kThreads, M::G, M::VS>(sm, tw, pp.p);
+    dif_full<A, LOG_R, kThreads, M::G, M::VS, kMaxRB>(sm, tw, pp.p);
     // Four-step twiddle w_T^(col * brev(row)) = fa * fb[col][brev(k)], then the store.
     u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + first;
     const uint2* fbc = fb + M::col() * (M::SWEEPS + 1);
@@ -362,14 +385,33 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
         for (int u = 0; u < B; ++u) sk[slot_offset<M::RS>(u)] = x[u];
     }
     __syncthreads();
-    dit_full<A, LOG_R, kThreads, M::G, M::VS>(sm, tw, pp.p);
-    q = base;
+    // Every inverse pass but the last in shared memory (the short one first) ...
+    constexpr int RB = kMaxRB;
+    constexpr int R0 = LOG_R % RB;
+    if constexpr (R0 > 0) {
+        dit_pass<A, LOG_R, 0, R0, kThreads, M::G, M::VS>(sm, tw, pp.p);
+        __syncthreads();
+    }
+    dit_range<A, LOG_R, kThreads, M::G, M::VS, R0, LOG_R - RB>(sm, tw, pp.p);
+    // ... and the last one straight to global memory as canonical residues. Item it
+    // takes column c = it mod G and block gg = it / G (rows gg + k * HS), so a warp
+    // reads distinct banks and writes four rows of G consecutive residues at a time.
+    {
+        constexpr int LOG_HS = LOG_R - RB, HS = 1 << LOG_HS;
+        u32* const out0 = m.spec + ((size_t)prime << g.log_t) + (blockIdx.x << M::LOG_G);
+        const u64 kstep = (u64)HS << g.log_c;
 #pragma unroll 1
-    for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
-        const u32* sk = s + slot_offset<M::RS>(k0);
+        for (int it = threadIdx.x; it < (M::G << LOG_HS); it += kThreads) {
+            const int c = it & (M::G - 1), gg = it >> M::LOG_G;
+            const u32* base = sm + c * M::VS + pad_index(gg);
+            u32 x[1][1 << RB];
 #pragma unroll
-        for (int u = 0; u < B; ++u) q[u * step] = A::canonical(sk[slot_offset<M::RS>(u)], pp.p);
-        q += B * step;
+            for (int k = 0; k < (1 << RB); ++k) x[0][k] = base[slot_offset<HS>(k)];
+            dit_levels<A, RB, HS, 1>(x, tw + gg, pp.p);
+            u32* out = out0 + ((u64)gg << g.log_c) + c;
+#pragma unroll
+            for (int k = 0; k < (1 << RB); ++k) out[k * kstep] = A::canonical(x[0][k], pp.p);
+        }
     }
 }
 
