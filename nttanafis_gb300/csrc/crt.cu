@@ -20,19 +20,17 @@ namespace ntt {
 
 constexpr int kCrtThreads = 256;
 
-// Reconstructs coefficient k from its residues: returns four u64 words of
-// S - q*P, S = sum_i y_i*(P/p_i), y_i = x_i*(P/p_i)^-1 mod p_i, q rounded from
-// sum_i y_i/p_i. Unsigned: 0 <= X < P/2. Signed: two's complement, |X| <= P/4.
+// Reconstructs X from its residues r_i: returns the NP + 1 u32 words (two's
+// complement) of X = S - q*P, S = sum_i y_i*(P/p_i), y_i = r_i*(P/p_i)^-1 mod p_i,
+// q rounded from sum_i y_i/p_i. Unsigned: 0 <= X < P/2. Signed: |X| <= P/4.
 template <int NP>
-__device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log_t, u64 k,
-                                          const CrtParams& cp, u64 out[4]) {
+__device__ __forceinline__ void crt_words(const u32 (&r)[NP], const CrtParams& cp, u32 (&x)[NP + 1]) {
     u32 y[NP];
     float f = 0.0f;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-        const u32 x = __ldg(resid + ((size_t)i << log_t) + k);
         const u32 p = cp.p[i];
-        u32 v = shoup_mul(x, cp.inv[i].x, cp.inv[i].y, p);
+        u32 v = shoup_mul(r[i], cp.inv[i].x, cp.inv[i].y, p);
         v = sub_if_ge(v, p);
         y[i] = v;
         f = fmaf((float)v, cp.pinv[i], f);
@@ -69,18 +67,36 @@ __device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log
 #pragma unroll
     for (int w = 2; w <= NP; ++w)
         asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[w]) : "r"(q), "r"(cp.P[w - 1]));
-    u32 x[NP + 1];
     asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(x[0]) : "r"(S[0]), "r"(U[0]));
 #pragma unroll
     for (int w = 1; w <= NP; ++w) asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(x[w]) : "r"(S[w]), "r"(U[w]));
+}
+
+// The first W u64 words of X (sign-filled above its NP + 1 u32 words).
+template <int NP, int W>
+__device__ __forceinline__ void pack_words(const u32 (&x)[NP + 1], u64 (&out)[W]) {
     const u64 fill = x[NP] ? ~0ull : 0ull;
 #pragma unroll
-    for (int w = 0; w < 4; ++w) {
+    for (int w = 0; w < W; ++w) {
         const int lo = 2 * w, hi = 2 * w + 1;
-        const u64 l = lo < NP ? (u64)x[lo] : (lo == NP ? (u64)x[NP] : fill & 0xffffffffull);
-        const u64 h = hi < NP ? (u64)x[hi] : (hi == NP ? (u64)x[NP] : fill & 0xffffffffull);
+        const u64 l = lo <= NP ? (u64)x[lo] : fill & 0xffffffffull;
+        const u64 h = hi <= NP ? (u64)x[hi] : fill & 0xffffffffull;
         out[w] = l | (h << 32);
     }
+}
+
+// Coefficient k of a residue array [prime][T] as four u64 words.
+template <int NP>
+__device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log_t, u64 k,
+                                          const CrtParams& cp, u64 out[4]) {
+    u32 r[NP], x[NP + 1];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) r[i] = __ldg(resid + ((size_t)i << log_t) + k);
+    crt_words<NP>(r, cp, x);
+    u64 w[4];
+    pack_words<NP, 4>(x, w);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) out[i] = w[i];
 }
 
 __device__ __forceinline__ void compose(u32& g, u32& p, u32 g_earlier, u32 p_earlier) {
@@ -172,18 +188,34 @@ __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin)
     return true;
 }
 
-// Tile of kCrtTile output limbs. Coefficient words sit in shared memory as four
-// word planes, so a warp reads consecutive 64-bit words. Warp w owns limbs
-// [128w, 128w + 128) of the tile; lane l handles limbs 32c + l of them (c < 4),
-// so every shared and global access of a warp is to consecutive words.
+// Tile of kCrtTile output limbs, four per thread: thread t reconstructs the
+// coefficients j0 + 4t .. j0 + 4t + 3 (coefficient k lands at limb k and spans L
+// limbs) and owns the limbs with the same indices. Limb j sums word w of coefficient
+// j - w for w < L; the words that come from the previous thread's coefficients
+// arrive by warp shuffle, or through shared memory across warps (the L coefficients
+// before the tile are reconstructed by threads 0..L-1). A limb's sum is a low word
+// plus an overflow count that joins the next limb; the carries that remain are
+// single bits, resolved per thread, by a warp scan, across warps, and across tiles
+// by the look-back.
 // flags: [0] tile counter, [1] error word, [2 + t] look-back state of tile t; all
 // zero when the kernel starts (the preceding transform kernel clears them).
+constexpr int kCrtPer = 4;
+static_assert(kCrtThreads * kCrtPer == kCrtTile, "four limbs per thread");
+
+// u64 words of a reconstructed coefficient for NP primes below 2^31 (X < 2^(31 NP - 1)).
+__host__ __device__ constexpr int crt_limb_words(int np) {
+    return (31 * np - 1 + 63) / 64 < 4 ? (31 * np - 1 + 63) / 64 : 4;
+}
+
 template <int NP>
 __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__ resid, int log_t,
                                                           u64 conv_len, u64 out_len, u64* __restrict__ dst,
                                                           u32* __restrict__ flags,
                                                           const __grid_constant__ CrtParams cp,
                                                           const ProductDesc* __restrict__ batch) {
+    constexpr int L = crt_limb_words(NP);
+    constexpr int NW = kCrtThreads / 32;
+    constexpr int NE = L * (L - 1) / 2;  // words a thread takes from its predecessor
     if (batch) {  // member blockIdx.y of a batch: grid.x covers its largest member
         const ProductDesc& d = batch[blockIdx.y];
         resid = d.spec;
@@ -195,78 +227,154 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
     // Tiles are numbered in the order CTAs start, so a tile only ever waits for
     // tiles whose CTAs are already running.
     __shared__ u32 s_tile, s_cin;
+    __shared__ u64 s_pre[L][L];              // the L coefficients before the tile
+    __shared__ u64 s_edge[NW][NE > 0 ? NE : 1];
+    __shared__ u32 s_edge_h[NW];
+    __shared__ u32 s_wg[NW], s_wp[NW];
     if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
     __syncthreads();
     const u32 tile = s_tile;
     const u32 tiles = (u32)((out_len + kCrtTile - 1) / kCrtTile);
     if (tile >= tiles) return;
-    constexpr int kBack = 4;  // coefficients before the tile that reach into it (l64 <= 4)
-    constexpr int kWords = kCrtTile + kBack;
-    constexpr int kChunks = kCrtTile / (32 * (kCrtThreads / 32));  // 4 chunks of 32 limbs per warp
-    __shared__ u64 xs[4][kWords];
-    __shared__ u32 wsum_g[32], wsum_p[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const u64 j0 = (u64)tile * kCrtTile;
-    for (int kk = threadIdx.x; kk < kWords; kk += kCrtThreads) {
-        const int64_t k = (int64_t)j0 - kBack + kk;
-        u64 w[4] = {0, 0, 0, 0};
-        if (k >= 0 && (u64)k < conv_len) crt_coeff<NP>(resid, log_t, (u64)k, cp, w);
-        xs[0][kk] = w[0];
-        xs[1][kk] = w[1];
-        xs[2][kk] = w[2];
-        xs[3][kk] = w[3];
+    const u64 k0 = j0 + (u64)t * kCrtPer;
+    // Coefficients k0 .. k0 + 3 (zero past the convolution).
+    u64 cw[kCrtPer][L];
+    {
+        u32 r[kCrtPer][NP];
+        if (k0 + kCrtPer <= conv_len && (reinterpret_cast<uintptr_t>(resid) & 15) == 0) {
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const uint4 v = __ldg(reinterpret_cast<const uint4*>(resid + ((size_t)i << log_t) + k0));
+                r[0][i] = v.x; r[1][i] = v.y; r[2][i] = v.z; r[3][i] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < kCrtPer; ++c)
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    r[c][i] = k0 + c < conv_len ? __ldg(resid + ((size_t)i << log_t) + k0 + c) : 0u;
+        }
+#pragma unroll
+        for (int c = 0; c < kCrtPer; ++c) {
+            u32 x[NP + 1];
+            crt_words<NP>(r[c], cp, x);
+            pack_words<NP, L>(x, cw[c]);
+        }
     }
-    __syncthreads();
-    const int L = cp.l64;
-    // Window sum of limb j0 + rel: low word and the count of its overflows.
-    auto limb_sum = [&](int rel, u32& hi) -> u64 {
+    if (t < L) {  // coefficient j0 - L + t, before the tile
+        u64 w[L];
+#pragma unroll
+        for (int i = 0; i < L; ++i) w[i] = 0;
+        if (j0 >= (u64)(L - t)) {
+            const u64 k = j0 - (u64)(L - t);
+            u32 r[NP], x[NP + 1];
+#pragma unroll
+            for (int i = 0; i < NP; ++i) r[i] = __ldg(resid + ((size_t)i << log_t) + k);
+            crt_words<NP>(r, cp, x);
+            pack_words<NP, L>(x, w);
+        }
+#pragma unroll
+        for (int i = 0; i < L; ++i) s_pre[t][i] = w[i];
+    }
+    // Sum of limb c from words of coefficients c - w (own when c - w >= 0, else
+    // from prev[]): low word and overflow count.
+    auto limb = [&](int c, const u64 (&prev)[NE > 0 ? NE : 1], u32& h) -> u64 {
         u64 lo = 0;
-        hi = 0;
+        h = 0;
+#pragma unroll
         for (int w = 0; w < L; ++w) {
-            const u64 v = xs[w][rel - w + kBack];
+            u64 v;
+            if (c - w >= 0) {
+                v = cw[c - w][w];
+            } else {
+                // pair (w, c) with c < w: index w(w-1)/2 + c
+                v = prev[w * (w - 1) / 2 + c];
+            }
             lo += v;
-            hi += (lo < v) ? 1u : 0u;
+            h += lo < v ? 1u : 0u;
         }
         return lo;
     };
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    u64 r[kChunks];
-    u32 eg[kChunks], ep[kChunks], cg[kChunks], cpp[kChunks];
-    u32 WG = 0, WP = 1;  // composite of this warp's chunks so far
-    u32 h_last = 0;      // overflow count of the previous chunk's last limb
-    if (lane == 0) limb_sum(warp * 32 * kChunks - 1, h_last);
-    h_last = __shfl_sync(0xffffffffu, h_last, 0);
+    // What the successor needs: words w of coefficients 4 + c - w (c < w) and the
+    // overflow count of limb 3 (own words only).
+    u64 mine[NE > 0 ? NE : 1];
 #pragma unroll
-    for (int c = 0; c < kChunks; ++c) {
-        const int rel = warp * 32 * kChunks + c * 32 + lane;
-        u32 h;
-        const u64 lo = limb_sum(rel, h);
-        u32 hprev = __shfl_up_sync(0xffffffffu, h, 1);
-        if (lane == 0) hprev = h_last;
-        h_last = __shfl_sync(0xffffffffu, h, 31);
-        const u64 s = lo + hprev;
-        r[c] = s;
-        u32 g = s < lo ? 1u : 0u, p = s == ~0ull ? 1u : 0u;
-        warp_scan_gp(g, p);
-        cg[c] = __shfl_sync(0xffffffffu, g, 31);
-        cpp[c] = __shfl_sync(0xffffffffu, p, 31);
-        u32 xg = __shfl_up_sync(0xffffffffu, g, 1), xp = __shfl_up_sync(0xffffffffu, p, 1);
-        if (lane == 0) { xg = 0; xp = 1; }
-        eg[c] = xg;
-        ep[c] = xp;
-        u32 ng = cg[c], np = cpp[c];
-        compose(ng, np, WG, WP);
-        WG = ng;
-        WP = np;
+    for (int w = 1; w < L; ++w)
+#pragma unroll
+        for (int c = 0; c < w; ++c) mine[w * (w - 1) / 2 + c] = cw[kCrtPer + c - w][w];
+    u32 h3;
+    {
+        const u64 dummy[NE > 0 ? NE : 1] = {};
+        limb(kCrtPer - 1, dummy, h3);  // limb 3 uses own words only (L <= 4)
     }
-    if (lane == 0) { wsum_g[warp] = WG; wsum_p[warp] = WP; }
+    if (lane == 31) {
+#pragma unroll
+        for (int e = 0; e < NE; ++e) s_edge[warp][e] = mine[e];
+        s_edge_h[warp] = h3;
+    }
+    __syncthreads();
+    u64 prev[NE > 0 ? NE : 1];
+    u32 hprev;
+#pragma unroll
+    for (int e = 0; e < NE; ++e) prev[e] = __shfl_up_sync(0xffffffffu, mine[e], 1);
+    hprev = __shfl_up_sync(0xffffffffu, h3, 1);
+    if (lane == 0) {
+        if (warp > 0) {
+#pragma unroll
+            for (int e = 0; e < NE; ++e) prev[e] = s_edge[warp - 1][e];
+            hprev = s_edge_h[warp - 1];
+        } else {
+            // predecessor = the coefficients before the tile: coefficient j0 - L + i
+            // plays the predecessor's coefficient 4 - L + i
+#pragma unroll
+            for (int w = 1; w < L; ++w)
+#pragma unroll
+                for (int c = 0; c < w; ++c) prev[w * (w - 1) / 2 + c] = s_pre[L + c - w][w];
+            // overflow count of limb j0 - 1: words w of coefficients j0 - 1 - w
+            u64 lo = 0;
+            hprev = 0;
+#pragma unroll
+            for (int w = 0; w < L; ++w) {
+                const u64 v = s_pre[L - 1 - w][w];
+                lo += v;
+                hprev += lo < v ? 1u : 0u;
+            }
+        }
+    }
+    // Limb values before the carries, and their (generate, propagate) bits.
+    u64 sv[kCrtPer];
+    u32 gb[kCrtPer], pb[kCrtPer];
+#pragma unroll
+    for (int c = 0; c < kCrtPer; ++c) {
+        u32 h;
+        const u64 lo = limb(c, prev, h);
+        const u64 s2 = lo + hprev;
+        sv[c] = s2;
+        gb[c] = s2 < lo ? 1u : 0u;
+        pb[c] = s2 == ~0ull ? 1u : 0u;
+        hprev = h;
+    }
+    // This thread's composite, then an inclusive warp scan of the composites.
+    u32 G = gb[0], P = pb[0];
+#pragma unroll
+    for (int c = 1; c < kCrtPer; ++c) {
+        G = gb[c] | (pb[c] & G);
+        P = pb[c] & P;
+    }
+    u32 ig = G, ip = P;
+    warp_scan_gp(ig, ip);
+    u32 xg = __shfl_up_sync(0xffffffffu, ig, 1), xp = __shfl_up_sync(0xffffffffu, ip, 1);
+    if (lane == 0) { xg = 0; xp = 1; }
+    if (lane == 31) { s_wg[warp] = ig; s_wp[warp] = ip; }
     __syncthreads();
     if (threadIdx.x == 0) {
         u32 tg = 0, tp = 1;  // the tile's (generate, propagate) pair
-        for (int w = 0; w < kCrtThreads / 32; ++w) {
-            u32 g = wsum_g[w], p = wsum_p[w];
-            compose(g, p, tg, tp);
-            tg = g;
-            tp = p;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            tg = s_wg[w] | (s_wp[w] & tg);
+            tp = s_wp[w] & tp;
         }
         u32* status = flags + 2;
         u32 cin = 0;
@@ -282,15 +390,25 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
         s_cin = cin;
     }
     __syncthreads();
-    // carry into this warp's first limb: the tile's carry-in through earlier warps
-    u32 cin = s_cin;
-    for (int w = 0; w < warp; ++w) cin = wsum_g[w] | (wsum_p[w] & cin);
+    // Carry into this thread's first limb: the tile's carry-in through the earlier
+    // warps, then through the earlier lanes of this warp.
+    u32 c = s_cin;
+    for (int w = 0; w < warp; ++w) c = s_wg[w] | (s_wp[w] & c);
+    c = xg | (xp & c);
+    u64 out[kCrtPer];
 #pragma unroll
-    for (int c = 0; c < kChunks; ++c) {
-        const u64 j = j0 + (u64)(warp * 32 * kChunks + c * 32 + lane);
-        const u32 carry = eg[c] | (ep[c] & cin);
-        if (j < out_len) dst[j] = r[c] + carry;
-        cin = cg[c] | (cpp[c] & cin);
+    for (int i = 0; i < kCrtPer; ++i) {
+        out[i] = sv[i] + c;
+        c = gb[i] | (pb[i] & c);
+    }
+    u64* d = dst + k0;
+    if (k0 + kCrtPer <= out_len && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+        reinterpret_cast<uint4*>(d)[0] = make_uint4((u32)out[0], (u32)(out[0] >> 32), (u32)out[1], (u32)(out[1] >> 32));
+        reinterpret_cast<uint4*>(d)[1] = make_uint4((u32)out[2], (u32)(out[2] >> 32), (u32)out[3], (u32)(out[3] >> 32));
+    } else {
+#pragma unroll
+        for (int i = 0; i < kCrtPer; ++i)
+            if (k0 + i < out_len) d[i] = out[i];
     }
 }
 
