@@ -87,9 +87,30 @@ __device__ __forceinline__ void dit_levels(u32 (&x)[VP][1 << RB], const uint2* _
     }
 }
 
+// Start of register block gg of a pass whose blocks span 2^RB points H apart:
+// i0 = a * H * 2^RB + j with j < H. With the plain order (j = gg mod H), a warp
+// whose 32 blocks have 2 <= H <= 16 covers 32 / H values of a, whose starts are H/2
+// banks apart in the padded layout: two-way conflicts. Taking H/2 values of j and
+// 64/H values of a per warp instead spreads the 32 starts over distinct banks (the
+// other half of j goes to the next warp).
+template <int LOG_H, int RB, int LOG_GPV>
+__device__ __forceinline__ int block_start(int gg, int& j) {
+    constexpr int H = 1 << LOG_H;
+    if constexpr (LOG_H >= 1 && LOG_H <= 4 && LOG_GPV >= 6) {
+        constexpr int LOG_HH = LOG_H - 1;  // log2(H / 2)
+        const int l = gg & 31, hi = gg >> 5;
+        j = ((hi & 1) << LOG_HH) + (l & ((1 << LOG_HH) - 1));
+        const int a = ((hi >> 1) << (6 - LOG_H)) + (l >> LOG_HH);
+        return (a << (LOG_H + RB)) + j;
+    } else {
+        j = gg & (H - 1);
+        return ((gg >> LOG_H) << (LOG_H + RB)) + j;
+    }
+}
+
 // One pass of RB forward levels starting at LEVEL over NV vectors of 2^LOG_N points,
-// VS words apart. Register block gg of a vector starts at point
-// i0 = (gg / HQ) * HQ * 2^RB + gg mod HQ and spans 2^RB points HQ apart.
+// VS words apart. Register block gg of a vector starts at block_start(gg) and spans
+// 2^RB points HQ apart.
 template <class A, int LOG_N, int LEVEL, int RB, int NT, int NV, int VS>
 __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __restrict__ tw, u32 p) {
     constexpr int E = 1 << RB;
@@ -102,8 +123,8 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __res
     for (int it = threadIdx.x; it < ITEMS; it += NT) {
         const int v = (it >> LOG_GPV) * VP;
         const int gg = it & ((1 << LOG_GPV) - 1);
-        const int j0 = gg & (HQ - 1);
-        const int i0 = ((gg >> LOG_HQ) << (LOG_HQ + RB)) + j0;
+        int j0;
+        const int i0 = block_start<LOG_HQ, RB, LOG_GPV>(gg, j0);
         u32* base = s + v * VS + pad_index(i0);
         u32 x[VP][E];
 #pragma unroll
@@ -119,7 +140,7 @@ __device__ __forceinline__ void dif_pass(u32* __restrict__ s, const uint2* __res
 }
 
 // One pass of RB inverse levels starting at LEVEL; block gg starts at
-// i0 = (gg / HS) * HS * 2^RB + gg mod HS with HS = 2^LEVEL.
+// block_start(gg) and spans 2^RB points HS = 2^LEVEL apart.
 template <class A, int LOG_N, int LEVEL, int RB, int NT, int NV, int VS>
 __device__ __forceinline__ void dit_pass(u32* __restrict__ s, const uint2* __restrict__ tw, u32 p) {
     constexpr int E = 1 << RB;
@@ -131,8 +152,8 @@ __device__ __forceinline__ void dit_pass(u32* __restrict__ s, const uint2* __res
     for (int it = threadIdx.x; it < ITEMS; it += NT) {
         const int v = (it >> LOG_GPV) * VP;
         const int gg = it & ((1 << LOG_GPV) - 1);
-        const int j0 = gg & (HS - 1);
-        const int i0 = ((gg >> LEVEL) << (LEVEL + RB)) + j0;
+        int j0;
+        const int i0 = block_start<LEVEL, RB, LOG_GPV>(gg, j0);
         u32* base = s + v * VS + pad_index(i0);
         u32 x[VP][E];
 #pragma unroll
