@@ -309,15 +309,22 @@ static bool prime_tables(int dev, u32 p, PrimeTables& out) {
     return true;
 }
 
-static u32 bit_reverse(u32 x, int bits) {
-    u32 r = 0;
-    for (int b = 0; b < bits; ++b) r |= ((x >> b) & 1u) << (bits - 1 - b);
-    return r;
+// Stream of the one-time table builds of each device (non-blocking, so a build
+// never waits for other work on the device).
+static std::map<int, cudaStream_t> g_table_streams;
+
+static cudaStream_t table_stream(int dev) {
+    auto it = g_table_streams.find(dev);
+    if (it != g_table_streams.end()) return it->second;
+    cudaStream_t st = nullptr;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate")) return nullptr;
+    g_table_streams[dev] = st;
+    return st;
 }
 
 // Root tables of one transform length: the inverse scale and, for the four-step
 // sizes, the forward and inverse twiddle factors in the layouts the column and row
-// passes read (launch.h describes them).
+// passes read (launch.h describes them), built by a kernel from the squares of w.
 static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
     auto key = std::make_tuple(dev, p, log_t);
     auto it = g_step_tables.find(key);
@@ -330,31 +337,32 @@ static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
     StepTables t;
     t.scale = shoup_pair(scale, p);
     if (log_t > kMaxBlockLog) {
-        const int log_r = log_t / 2, log_c = log_t - log_r;
-        const u64 R = (u64)1 << log_r, C = (u64)1 << log_c;
-        const u64 RS = (u64)1 << kColLogRS, SW = R / RS;
-        const u64 NL = (u64)1 << kRowTwLoBits, NH = C >> kRowTwLoBits;
-        std::vector<uint2> fa(C * RS), fb(C * SW), ilo(R * NL), ihi(R * NH);
-        const u32 w_sw = powmod(w, SW, p);
-        u32 wc = 1, wc_sw = 1;  // w^col and w^(col * SW)
-        for (u64 col = 0; col < C; ++col) {
-            u32 x = 1;
-            for (u64 u = 0; u < RS; ++u, x = mulmod(x, wc_sw, p)) fa[col * RS + u] = shoup_pair(x, p);
-            x = 1;
-            for (u64 j = 0; j < SW; ++j, x = mulmod(x, wc, p)) fb[col * SW + j] = shoup_pair(x, p);
-            wc = mulmod(wc, w, p);
-            wc_sw = mulmod(wc_sw, w_sw, p);
+        StepTableBuild b;
+        memset(&b, 0, sizeof(b));
+        b.p = p;
+        b.log_t = log_t;
+        b.log_r = log_t / 2;
+        b.log_c = log_t - b.log_r;
+        u32 x = w, ix = iw;
+        for (int i = 0; i <= log_t; ++i) {
+            b.fwd_pow[i] = shoup_pair(x, p);
+            b.inv_pow[i] = shoup_pair(ix, p);
+            x = mulmod(x, x, p);
+            ix = mulmod(ix, ix, p);
         }
-        for (u64 row = 0; row < R; ++row) {
-            const u32 c = powmod(iw, bit_reverse((u32)row, log_r), p);  // w^-k1
-            u32 x = 1;
-            for (u64 lo = 0; lo < NL; ++lo, x = mulmod(x, c, p))
-                ilo[row * NL + lo] = shoup_pair(x, p);
-            const u32 c64 = x;  // w^(-k1 * 64)
-            x = scale;
-            for (u64 hi = 0; hi < NH; ++hi, x = mulmod(x, c64, p)) ihi[row * NH + hi] = shoup_pair(x, p);
-        }
-        if (!upload(&t.f_a, fa) || !upload(&t.f_b, fb) || !upload(&t.i_lo, ilo) || !upload(&t.i_hi, ihi))
+        b.scale = t.scale;
+        u64 n[4];
+        step_table_sizes(log_t, n);
+        uint2** dst[4] = {&t.f_a, &t.f_b, &t.i_lo, &t.i_hi};
+        for (int i = 0; i < 4; ++i)
+            if (!cuda_ok(cudaMalloc((void**)dst[i], n[i] * sizeof(uint2)), "cudaMalloc(table)")) return false;
+        b.f4_a = t.f_a;
+        b.f4_b = t.f_b;
+        b.i4_lo = t.i_lo;
+        b.i4_hi = t.i_hi;
+        cudaStream_t st = table_stream(dev);
+        if (!st || !cuda_ok(launch_step_tables(b, st), "table build launch") ||
+            !cuda_ok(cudaStreamSynchronize(st), "table build"))
             return false;
     }
     g_step_tables[key] = t;

@@ -109,6 +109,28 @@ cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_c
                                   const CrtParams& cp, cudaStream_t st);
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
                                    int stride, bool sign, cudaStream_t st);
+// Four-step factor tables of one prime and transform length, built on the GPU:
+// every entry is a power of w (forward) or w^-1 (inverse) with its Shoup companion,
+// computed from the squares w^(2^i) (with companions) given here.
+struct StepTableBuild {
+    u32 p;
+    int log_t, log_r, log_c;
+    uint2 fwd_pow[kMaxLogT + 1];  // w^(2^i), i <= log_t
+    uint2 inv_pow[kMaxLogT + 1];  // w^(-2^i)
+    uint2 scale;                  // inverse scale folded into i4_hi
+    uint2 *f4_a, *f4_b, *i4_lo, *i4_hi;
+};
+// Entries of the four tables (in the order f4_a, f4_b, i4_lo, i4_hi).
+__host__ __device__ inline void step_table_sizes(int log_t, u64 sizes[4]) {
+    const int log_r = log_t / 2, log_c = log_t - log_r;
+    const u64 R = (u64)1 << log_r, C = (u64)1 << log_c;
+    sizes[0] = C << kColLogRS;                     // f4_a: [col][brev(r0)]
+    sizes[1] = C * (R >> kColLogRS);               // f4_b: [col][sweep]
+    sizes[2] = R << kRowTwLoBits;                  // i4_lo: [row][lo]
+    sizes[3] = R * (C >> kRowTwLoBits);            // i4_hi: [row][hi]
+}
+cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st);
+
 // Scratch bytes of the CRT look-back flags for `out_len` output limbs: a tile
 // counter, an error word and one state word per tile of kCrtTile limbs.
 __host__ __device__ inline u64 carry_flag_words(u64 out_len) { return 2 + (out_len + kCrtTile - 1) / kCrtTile; }

@@ -19,6 +19,8 @@
 #include "launch.h"
 #include "ntt_passes.cuh"
 
+#include <algorithm>
+
 namespace ntt {
 
 constexpr int kThreads = kColThreads;
@@ -413,6 +415,62 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
             for (int k = 0; k < (1 << RB); ++k) out[k * kstep] = A::canonical(x[0][k], pp.p);
         }
     }
+}
+
+// ---------------------------------------------------------------------------------
+// Four-step factor tables (layouts in launch.h). One thread per entry: the exponent
+// of the entry, then the power as a product of the tabulated squares (Shoup
+// products by constants), then its companion floor(x * 2^32 / p).
+
+__device__ __forceinline__ u32 power_of(const uint2* pow2, u64 e, int bits, u32 p) {
+    u32 x = 1;
+    for (int i = 0; i < bits; ++i)
+        if ((e >> i) & 1) x = sub_if_ge(shoup_mul(x, pow2[i].x, pow2[i].y, p), p);
+    return x;
+}
+
+__global__ void __launch_bounds__(256) k_step_tables(const __grid_constant__ StepTableBuild b) {
+    u64 n[4];
+    step_table_sizes(b.log_t, n);
+    const u64 mask = ((u64)1 << b.log_t) - 1;
+    const int log_sw = b.log_r - kColLogRS, log_nh = b.log_c - kRowTwLoBits;
+    const u64 total = n[0] + n[1] + n[2] + n[3];
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+        u64 k = i;
+        u32 x;
+        uint2* out;
+        if (k < n[0]) {  // w^(col * u * SW)
+            const u64 col = k >> kColLogRS, u = k & ((1u << kColLogRS) - 1);
+            x = power_of(b.fwd_pow, ((col * u) << log_sw) & mask, b.log_t, b.p);
+            out = b.f4_a + k;
+        } else if ((k -= n[0]) < n[1]) {  // w^(col * j)
+            const u64 col = k >> log_sw, j = k & (((u64)1 << log_sw) - 1);
+            x = power_of(b.fwd_pow, (col * j) & mask, b.log_t, b.p);
+            out = b.f4_b + k;
+        } else if ((k -= n[1]) < n[2]) {  // w^(-k1 * lo)
+            const u64 row = k >> kRowTwLoBits, lo = k & ((1u << kRowTwLoBits) - 1);
+            const u64 k1 = __brev((u32)row) >> (32 - b.log_r);
+            x = power_of(b.inv_pow, (k1 * lo) & mask, b.log_t, b.p);
+            out = b.i4_lo + k;
+        } else {  // w^(-k1 * 64 * hi) * scale
+            k -= n[2];
+            const u64 row = k >> log_nh, hi = k & (((u64)1 << log_nh) - 1);
+            const u64 k1 = __brev((u32)row) >> (32 - b.log_r);
+            x = power_of(b.inv_pow, ((k1 * hi) << kRowTwLoBits) & mask, b.log_t, b.p);
+            x = sub_if_ge(shoup_mul(x, b.scale.x, b.scale.y, b.p), b.p);
+            out = b.i4_hi + k;
+        }
+        *out = make_uint2(x, (u32)(((u64)x << 32) / b.p));
+    }
+}
+
+cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st) {
+    u64 n[4];
+    step_table_sizes(b.log_t, n);
+    const u64 total = n[0] + n[1] + n[2] + n[3];
+    const unsigned blocks = (unsigned)std::min<u64>((total + 255) / 256, 152 * 16);
+    k_step_tables<<<blocks, 256, 0, st>>>(b);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------------
