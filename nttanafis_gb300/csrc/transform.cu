@@ -242,6 +242,114 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     }
 }
 
+// Column passes for R = 2^10 (every product with T = 2^20 or 2^21, the 1M x 1M
+// bench shape among them) in two radix-32 passes: one barrier and one round trip
+// through shared memory per element. A thread owns one register block per pass:
+// column c = t mod 8 and either rows gg + 32k (block gg) or rows 32 g2 + k (block
+// g2), k < 32. With the padded column stride (4 mod 32) both orders put a warp's
+// 8 columns x 4 blocks on 32 distinct banks, and both read or write global memory
+// as 4 rows x 8 consecutive columns. The forward four-step twiddle of row
+// 32 g2 + k is w_T^(col * brev(row)) = f4_a[col][brev5(k)] * f4_b[col][brev5(g2)]
+// (brev(row) = 32 brev5(k) + brev5(g2)). Four CTAs per SM (64 registers) measured
+// best.
+constexpr int kCol2LogR = 10;
+static_assert(kColLogG == 3 && kColLogRS == 5, "two-pass columns assume 8 columns per CTA");
+
+template <class A, bool SIGNED>
+__global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant__ TransformArgs g) {
+    extern __shared__ u32 sm[];
+    constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
+    const int prime = blockIdx.y;
+    const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z + g.op_base;
+    const Member m = member_of(g, g.batch ? (blockIdx.z >> 1) : 0, false);
+    if (op && m.square) return;
+    const PrimeParams& pp = g.ps.pr[prime];
+    const u64* __restrict__ src = op ? m.b : m.a;
+    const u64 len = op ? m.lb : m.la;
+    const int log_c = g.log_c;
+    const u32 col0 = (u32)(blockIdx.x * G);
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    const u32 col = col0 + c;
+    // f4_a rows of the CTA's columns, padded to 33 entries per column.
+    uint2* fa = reinterpret_cast<uint2*>(sm + G * VS);
+    fa[c * (E + 1) + blk] = __ldg(pp.f4_a + ((size_t)col << 5) + blk);
+    // Pass 1: levels 0-4 on rows blk + 32k, limbs reduced on the way in; rows R/2
+    // and above hold no limb when len <= T/2.
+    {
+        const bool half = len <= ((u64)1 << (g.log_t - 1));
+        const u64* p0 = src + ((u64)blk << log_c) + col;
+        const u64 n0 = ((u64)blk << log_c) + col, kstep = (u64)E << log_c;
+        u32 x[1][E];
+        if (half) {
+#pragma unroll
+            for (int k = 0; k < E / 2; ++k)
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            dif_levels<A, 5, E, 1, true>(x, pp.fwd + blk, pp.p);
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; ++k)
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            dif_levels<A, 5, E, 1>(x, pp.fwd + blk, pp.p);
+        }
+        u32* base = sm + c * VS + blk;
+#pragma unroll
+        for (int k = 0; k < E; ++k) base[33 * k] = x[0][k];
+    }
+    __syncthreads();
+    // Pass 2: levels 5-9 on rows 32 blk + k, four-step twiddle, store.
+    {
+        const u32* base = sm + c * VS + 33 * blk;
+        u32 x[1][E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) x[0][k] = base[k];
+        dif_levels<A, 5, 1, 1>(x, pp.fwd, pp.p);
+        const uint2 fb = __ldg(pp.f4_b + ((size_t)col << 5) + (__brev((u32)blk) >> 27));
+        const uint2* fac = fa + c * (E + 1);
+        u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + ((u64)(blk * E) << log_c) + col;
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+            const u32 y = A::mulc(A::mulc(x[0][k], fac[__brev((u32)k) >> 27], pp.p), fb, pp.p);
+            dst[(u64)k << log_c] = y;
+        }
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant__ TransformArgs g) {
+    extern __shared__ u32 sm[];
+    constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
+    const int prime = blockIdx.y;
+    const PrimeParams& pp = g.ps.pr[prime];
+    const Member m = member_of(g, blockIdx.z, false);
+    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
+    const int log_c = g.log_c;
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    u32* const spec = m.spec + ((size_t)prime << g.log_t) + blockIdx.x * G + c;
+    // Pass 1: levels 0-4 on rows 32 blk + k (bit-reversed spectrum in).
+    {
+        const u32* q = spec + ((u64)(blk * E) << log_c);
+        u32 x[1][E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) x[0][k] = __ldcs(q + ((u64)k << log_c));
+        dit_levels<A, 5, 1, 1>(x, pp.inv, pp.p);
+        u32* base = sm + c * VS + 33 * blk;
+#pragma unroll
+        for (int k = 0; k < E; ++k) base[k] = x[0][k];
+    }
+    __syncthreads();
+    // Pass 2: levels 5-9 on rows blk + 32k, canonical residues out.
+    {
+        const u32* base = sm + c * VS + blk;
+        u32 x[1][E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) x[0][k] = base[33 * k];
+        dit_levels<A, 5, E, 1>(x, pp.inv + blk, pp.p);
+        u32* q = spec + ((u64)blk << log_c);
+#pragma unroll
+        for (int k = 0; k < E; ++k) q[(u64)(k * E) << log_c] = A::canonical(x[0][k], pp.p);
+    }
+}
+
 // Rows per CTA of the row pass: enough that every thread owns a register block of
 // the first pass (2^(log_c - kMaxRB) blocks per row).
 __host__ __device__ constexpr int row_log_rpc(int log_c) {
@@ -524,14 +632,25 @@ static cudaError_t small_at(const TransformArgs& g, bool square, bool sign, cuda
     return cudaGetLastError();
 }
 
+// Column data plus the f4_a rows of the two-pass forward kernel.
+static size_t col2_smem(bool fwd) {
+    const size_t words = (size_t)col_vstride(kCol2LogR) * 8;
+    return ((words * sizeof(u32) + 15) & ~(size_t)15) + (fwd ? 8 * 8 * 33 : 0);
+}
+
 template <class A, int L>
 static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
-    auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
-    if (init) return opt_in(k, NTT_COLS_CARVEOUT);
     const unsigned ops = g.op_count ? g.op_count : (square ? 1 : 2);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : ops);
-    const size_t smem = col_smem(L, true);
-    k<<<grid, kThreads, smem, st>>>(g);
+    if constexpr (L == kCol2LogR) {
+        auto k = sign ? k_fwd_cols2<A, true> : k_fwd_cols2<A, false>;
+        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        k<<<grid, kThreads, col2_smem(true), st>>>(g);
+    } else {
+        auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
+        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        k<<<grid, kThreads, col_smem(L, true), st>>>(g);
+    }
     return cudaGetLastError();
 }
 
@@ -547,11 +666,16 @@ static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st,
 
 template <class A, int L>
 static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool init) {
-    auto k = k_inv_cols<A, L>;
-    if (init) return opt_in(k, NTT_COLS_CARVEOUT);
     const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? g.count : 1);
-    const size_t smem = col_smem(L, false);
-    k<<<grid, kThreads, smem, st>>>(g);
+    if constexpr (L == kCol2LogR) {
+        auto k = k_inv_cols2<A>;
+        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        k<<<grid, kThreads, col2_smem(false), st>>>(g);
+    } else {
+        auto k = k_inv_cols<A, L>;
+        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        k<<<grid, kThreads, col_smem(L, false), st>>>(g);
+    }
     return cudaGetLastError();
 }
 
