@@ -18,7 +18,7 @@
 
 namespace ntt {
 
-constexpr int kCrtThreads = 256;
+constexpr int kCrtThreads = kCrtTile / 4;
 
 // Reconstructs X from its residues r_i: returns the NP + 1 u32 words (two's
 // complement) of X = S - q*P, S = sum_i y_i*(P/p_i), y_i = r_i*(P/p_i)^-1 mod p_i,

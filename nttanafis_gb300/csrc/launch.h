@@ -14,8 +14,11 @@ namespace ntt {
 constexpr int kMaxBlockLog = 13;
 // Largest transform length handled at all (coefficients of a product or convolution).
 constexpr int kMaxLogT = 25;
-// Output limbs per CTA of the CRT + carry kernel.
-constexpr int kCrtTile = 1024;
+// Output limbs per CTA of the CRT + carry kernel (four per thread).
+#ifndef NTT_CRT_TILE
+#define NTT_CRT_TILE 1024
+#endif
+constexpr int kCrtTile = NTT_CRT_TILE;
 
 // Column passes of the four-step: a CTA of kColThreads threads owns 2^kColLogG
 // columns; thread t takes column t mod 2^kColLogG and rows r0 + k * RS with
