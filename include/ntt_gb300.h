@@ -53,6 +53,8 @@ typedef struct ntt_mul_plan {
     uint32_t log_transform;   /* log2 of the transform length */
     uint64_t scratch_len;     /* device scratch limbs of ntt_mul_plan_mul_device */
     uint64_t sqr_scratch_len; /* device scratch limbs of ntt_mul_plan_sqr_device */
+    uint64_t block_len;       /* block split: limbs per block of the longer operand (0: none) */
+    uint64_t blocks;          /* block split: blocks of the longer operand */
 } ntt_mul_plan;
 
 /* Admitted convolution geometry (ConvPlan). */
@@ -74,8 +76,12 @@ typedef struct ntt_mul_workspace ntt_mul_workspace;
 typedef struct ntt_conv_workspace ntt_conv_workspace;
 
 /* Plans positive lengths; returns 0 (no plan) for a zero length or a shape beyond
- * the GPU transform catalog (a_len + b_len - 1 > 2^25 coefficients). MulPlan::new,
- * src/plan.rs:53. */
+ * the GPU transform catalog: a_len + b_len - 1 > 2^25 coefficients unless the
+ * product takes the block split (the longer operand in blocks, each multiplied by
+ * the shorter one; shorter operand up to 2^24 limbs, longer up to 2^40). A very
+ * unbalanced product takes the split whenever it is cheaper (log_transform is then
+ * the block transform). MulPlan::new, src/plan.rs:53; the split follows
+ * Geometry::cheapest_blocks, src/profile/planner.rs:291. */
 int ntt_mul_plan_new(uint64_t len_a, uint64_t len_b, ntt_mul_plan* out);
 
 /* a*b into d_dst with caller-owned device scratch (MulPlan::mul, src/plan.rs:94). */

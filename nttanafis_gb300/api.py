@@ -35,6 +35,8 @@ class NttMulPlan(ctypes.Structure):
         ("log_transform", ctypes.c_uint32),
         ("scratch_len", ctypes.c_uint64),
         ("sqr_scratch_len", ctypes.c_uint64),
+        ("block_len", ctypes.c_uint64),
+        ("blocks", ctypes.c_uint64),
     ]
 
 
@@ -179,6 +181,8 @@ class MulPlan:
     log_transform: int
     scratch_len_limbs: int
     sqr_scratch_len_limbs: int
+    block_len: int = 0  # block split: limbs per block of the longer operand (0: none)
+    blocks: int = 0
 
     @staticmethod
     def new(len_a: int, len_b: int) -> Optional["MulPlan"]:
@@ -186,7 +190,7 @@ class MulPlan:
         if not library().ntt_mul_plan_new(len_a, len_b, ctypes.byref(raw)):
             return None
         return MulPlan(raw.len_a, raw.len_b, raw.primes, raw.log_transform, raw.scratch_len,
-                       raw.sqr_scratch_len)
+                       raw.sqr_scratch_len, raw.block_len, raw.blocks)
 
     def scratch_len(self) -> int:
         return self.scratch_len_limbs
@@ -196,7 +200,7 @@ class MulPlan:
 
     def _raw(self) -> NttMulPlan:
         return NttMulPlan(self.len_a, self.len_b, self.primes, self.log_transform, self.scratch_len_limbs,
-                          self.sqr_scratch_len_limbs)
+                          self.sqr_scratch_len_limbs, self.block_len, self.blocks)
 
     def mul_device(self, dst, a, b, scratch, stream=None) -> bool:
         """a*b on device tensors with caller-owned device scratch (MulPlan::mul)."""

@@ -151,6 +151,9 @@ static int capacity(const std::vector<u32>& primes, int np) {
 
 static int ceil_log2(u64 x) { return x <= 1 ? 0 : 64 - __builtin_clzll(x - 1); }
 
+// Smallest block transform of a split product (2^10 points).
+constexpr int kSmallSplitLog = 10;
+
 // ---------------------------------------------------------------------------------
 // Plans
 
@@ -163,11 +166,32 @@ struct Geom {
     u64 max_a = 0, max_b = 0;
     int sign = 0, bound_bits = 0, schoolbook = 0;
     u64 stride = 1;
+    // block split of an unbalanced product: the longer operand in blocks of `block`
+    // limbs, each multiplied by the shorter one with transforms of 2^log_t points
+    u64 block = 0, blocks = 0;
 
     bool matches(u64 a, u64 b) const { return a == la && b == lb; }
+    bool split() const { return block != 0; }
     u64 spec_words(bool square) const { return (u64)(square ? 1 : 2) * np * ((u64)1 << log_t); }
+    // residues and carry flags of one product of this geometry (one block if split)
+    u64 member_bytes(bool square) const {
+        const u64 spec = (spec_words(square) * 4 + 255) & ~(u64)255;
+        const u64 out = split() ? block + std::min(la, lb) : out_len;
+        return spec + ((conv ? 0 : carry_scratch_bytes(out)) + 255 & ~(u64)255);
+    }
+    // blocks per enqueue of a split product: bounded launch grids and arena
+    u64 split_chunk() const {
+        const u64 by_bytes = std::max<u64>(1, ((u64)512 << 20) / member_bytes(false));
+        return std::min<u64>({blocks, 16384, by_bytes});
+    }
+    // split: [descriptors][odd-block sums (out_len limbs)][add flags][member arenas]
+    u64 split_desc_bytes() const { return (split_chunk() * sizeof(ProductDesc) + 255) & ~(u64)255; }
+    u64 split_odd_bytes() const { return (out_len * 8 + 255) & ~(u64)255; }
+    u64 split_flag_bytes() const { return (carry_scratch_bytes(out_len) + 255) & ~(u64)255; }
     u64 scratch_bytes(bool square) const {
         if (conv && schoolbook) return 0;
+        if (split())
+            return split_desc_bytes() + split_odd_bytes() + split_flag_bytes() + split_chunk() * member_bytes(false);
         const u64 spec = (spec_words(square) * 4 + 255) & ~(u64)255;
         return spec + (conv ? 0 : carry_scratch_bytes(out_len));
     }
@@ -188,18 +212,54 @@ static bool choose_primes(Geom& g, int need_bits) {
     return false;
 }
 
-static bool plan_mul(u64 la, u64 lb, Geom& g) {
+// Longest operand of a split product (limbs).
+constexpr u64 kMaxSplitLimbs = (u64)1 << 40;
+
+// Block split of an unbalanced product (the reference's Geometry::cheapest_blocks,
+// src/profile/planner.rs:291-393, restated for this library's transforms): the
+// longer operand (L limbs) in blocks of B = 2^k - S + 1 limbs, each multiplied by
+// the shorter one (S limbs) with 2^k-point transforms. Cost in butterfly levels:
+// three transforms per block, n * 3 * 2^k * k, against 3 * 2^K * K for one
+// transform of the whole product. Returns the chosen k, or 0 when one transform
+// is cheaper (by the margin that pays for the block sums and the final addition).
+static int split_log(u64 L, u64 S, int full_log) {
+    const double full = full_log <= kMaxLogT ? 3.0 * std::ldexp(1.0, full_log) * full_log : 1e300;
+    int best_k = 0;
+    double best = 0.8 * full;
+    const int lo = std::max(kSmallSplitLog, ceil_log2(2 * S));
+    for (int k = lo; k <= kMaxLogT && k < full_log; ++k) {
+        const u64 B = ((u64)1 << k) - S + 1;
+        const double n = (double)((L + B - 1) / B);
+        const double cost = n * 3.0 * std::ldexp(1.0, k) * k;
+        if (cost < best) {
+            best = cost;
+            best_k = k;
+        }
+    }
+    return best_k;
+}
+
+// allow_split: callers that run one product per call (workspaces, plans) may take
+// the block split; batch members always use one transform.
+static bool plan_mul(u64 la, u64 lb, Geom& g, bool allow_split = true) {
     if (!la || !lb) return fail("operand length is zero");
-    if (la > ((u64)1 << kMaxLogT) || lb > ((u64)1 << kMaxLogT) ||
-        la + lb - 1 > ((u64)1 << kMaxLogT))
-        return fail("product exceeds 2^25 transform coefficients");
+    const u64 L = std::max(la, lb), S = std::min(la, lb);
+    const int full_log = std::max(4, ceil_log2(la + lb - 1));
+    int k = allow_split && L <= kMaxSplitLimbs ? split_log(L, S, full_log) : 0;
+    if (!k && full_log > kMaxLogT)
+        return fail(allow_split ? "product exceeds 2^25 transform coefficients and admits no block split"
+                                : "product exceeds 2^25 transform coefficients");
     g = Geom();
     g.la = la;
     g.lb = lb;
     g.conv_len = la + lb - 1;
     g.out_len = la + lb;
-    g.log_t = std::max(4, ceil_log2(g.conv_len));
-    const int need = 128 + ceil_log2(std::min(la, lb));
+    g.log_t = k ? k : full_log;
+    if (k) {
+        g.block = ((u64)1 << k) - S + 1;
+        g.blocks = (L + g.block - 1) / g.block;
+    }
+    const int need = 128 + ceil_log2(S);
     if (!choose_primes(g, need)) return fail("no prime set holds the coefficients");
     return true;
 }
@@ -432,12 +492,83 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
 // ---------------------------------------------------------------------------------
 // Execution on device pointers
 
+// Enqueues the kernels of `n` members of one transform class (same kind, length,
+// primes, sign and square) whose descriptors sit in device memory; max_len is the
+// longest member output (limbs of a product, coefficients of a convolution).
+static bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st) {
+    TransformArgs ta;
+    memset(&ta, 0, sizeof(ta));
+    CrtParams cp;
+    if (!prepare_params(g0, ta.ps, cp)) return false;
+    ta.batch = descs;
+    ta.count = n;
+    ta.np = g0.np;
+    ta.log_t = g0.log_t;
+    ta.wide = g0.wide;
+    const bool sign = g0.sign != 0;
+    if (g0.log_t <= kMaxBlockLog) {
+        g_launches += 1;
+        if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return false;
+    } else {
+        ta.log_r = g0.log_t / 2;
+        ta.log_c = g0.log_t - ta.log_r;
+        g_launches += 3;
+        if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch") ||
+            !cuda_ok(launch_rows(ta, sq, st), "batched row pass launch") ||
+            !cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch"))
+            return false;
+    }
+    g_launches += 1;
+    if (g0.conv)
+        return cuda_ok(launch_crt_conv_batch(descs, n, max_len, g0.log_t, cp, st), "batched CRT launch");
+    return cuda_ok(launch_crt_mul_batch(descs, n, (int)((max_len + kCrtTile - 1) / kCrtTile), g0.log_t, cp, st),
+                   "batched CRT launch");
+}
+
+// Enqueues a split product: the blocks of the longer operand times the shorter one
+// as batch members in chunks (the even blocks' products straight into dst, the odd
+// ones' into a second number), then dst += odd with carries.
+static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_dst, void* scratch, cudaStream_t st) {
+    const bool swap = g.la < g.lb;
+    const u64* lng = swap ? d_b : d_a;
+    const u64* sht = swap ? d_a : d_b;
+    const u64 L = std::max(g.la, g.lb), S = std::min(g.la, g.lb);
+    uint8_t* base = (uint8_t*)scratch;
+    ProductDesc* descs = (ProductDesc*)base;
+    u64* odd = (u64*)(base + g.split_desc_bytes());
+    u32* flags = (u32*)((uint8_t*)odd + g.split_odd_bytes());
+    uint8_t* arena = (uint8_t*)flags + g.split_flag_bytes();
+    const u64 member = g.member_bytes(false), spec = (g.spec_words(false) * 4 + 255) & ~(u64)255;
+    if (!cuda_ok(cudaMemsetAsync(d_dst, 0, g.out_len * 8, st), "zero product") ||
+        !cuda_ok(cudaMemsetAsync(odd, 0, g.out_len * 8, st), "zero odd blocks") ||
+        !cuda_ok(cudaMemsetAsync(flags, 0, carry_scratch_bytes(g.out_len), st), "zero carry flags"))
+        return false;
+    const u64 chunk = g.split_chunk();
+    for (u64 first = 0; first < g.blocks; first += chunk) {
+        const u64 count = std::min(chunk, g.blocks - first);
+        g_launches += 1;
+        if (!cuda_ok(launch_split_descs(descs, first, count, lng, L, sht, S, g.block, d_dst, odd, arena, member, spec,
+                                        st),
+                     "split descriptors") ||
+            !run_members(descs, (int)count, g, false, g.block + S, st))
+            return false;
+    }
+    g_launches += 1;
+    return cuda_ok(launch_add_limbs(d_dst, odd, g.out_len, flags, st), "block sum");
+}
+
 // Enqueues one product or convolution on `st`. With `b_ready` set (an event that
 // completes when operand b is in place), the column pass of a runs first and the
 // one of b waits for that event, so b's upload overlaps a's pass.
 static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst,
                     void* scratch, cudaStream_t st, cudaEvent_t b_ready = nullptr) {
     mark(st);
+    if (g.split()) {
+        if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
+        const bool ok = execute_split(g, d_a, square ? d_a : d_b, d_dst, scratch, st);
+        mark(st);
+        return ok;
+    }
     if (g.conv && g.schoolbook) {
         g_launches += 1;
         const bool ok = cuda_ok(launch_conv_schoolbook(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst,
@@ -623,7 +754,8 @@ static void* mapped_host_pointer(void* p) {
 template <class W>
 static bool run_host(W* ws, const Geom& g, bool square, u64* dst, const u64* a, const u64* b) {
     const size_t out_bytes = g.out_len * sizeof(u64);
-    u64* direct = (u64*)mapped_host_pointer(dst);
+    // a split product adds into its destination: keep that in device memory
+    u64* direct = g.split() ? nullptr : (u64*)mapped_host_pointer(dst);
     if (!ws->a.ensure(g.la * 8) || (!square && !ws->b.ensure(g.lb * 8)) || (!direct && !ws->out.ensure(out_bytes)) ||
         !ws->scratch.ensure(g.scratch_bytes(square)))
         return false;
@@ -655,6 +787,8 @@ int ntt_mul_plan_new(uint64_t len_a, uint64_t len_b, ntt_mul_plan* out) {
     out->log_transform = (uint32_t)g.log_t;
     out->scratch_len = (g.scratch_bytes(false) + 7) / 8;
     out->sqr_scratch_len = (g.scratch_bytes(true) + 7) / 8;
+    out->block_len = g.block;
+    out->blocks = g.blocks;
     return 1;
 }
 
@@ -960,7 +1094,7 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
                 empties.push_back(i);
                 continue;
             }
-            if (!plan_mul(r.a_len, r.b_len, m.g)) return 0;
+            if (!plan_mul(r.a_len, r.b_len, m.g, false)) return 0;
         } else if (r.kind == 1) {
             if (!plan_conv(r.a_len, r.b_len, r.max_a, r.max_b, (int)r.is_signed, m.g)) return 0;
         } else {
@@ -1041,43 +1175,10 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
             k = end;
             continue;
         }
-        TransformArgs ta;
-        memset(&ta, 0, sizeof(ta));
-        CrtParams cp;
-        if (!prepare_params(g0, ta.ps, cp)) return 0;
-        ta.batch = dev_desc + k;
-        ta.count = n;
-        ta.np = g0.np;
-        ta.log_t = g0.log_t;
-        ta.wide = g0.wide;
-        const bool sign = g0.sign != 0;
-        if (g0.log_t <= kMaxBlockLog) {
-            g_launches += 1;
-            if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return 0;
-        } else {
-            ta.log_r = g0.log_t / 2;
-            ta.log_c = g0.log_t - ta.log_r;
-            g_launches += 3;
-            if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch") ||
-                !cuda_ok(launch_rows(ta, sq, st), "batched row pass launch") ||
-                !cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch"))
-                return 0;
-        }
-        if (g0.conv) {
-            u64 max_conv = 0;
-            for (size_t i = k; i < end; ++i) max_conv = std::max(max_conv, members[i].g.conv_len);
-            g_launches += 1;
-            if (!cuda_ok(launch_crt_conv_batch(dev_desc + k, n, max_conv, g0.log_t, cp, st), "batched CRT launch"))
-                return 0;
-        } else {
-            u64 max_out = 0;
-            for (size_t i = k; i < end; ++i) max_out = std::max(max_out, members[i].g.out_len);
-            g_launches += 1;
-            if (!cuda_ok(launch_crt_mul_batch(dev_desc + k, n, (int)((max_out + kCrtTile - 1) / kCrtTile), g0.log_t,
-                                              cp, st),
-                         "batched CRT launch"))
-                return 0;
-        }
+        u64 max_len = 0;
+        for (size_t i = k; i < end; ++i)
+            max_len = std::max(max_len, g0.conv ? members[i].g.conv_len : members[i].g.out_len);
+        if (!run_members(dev_desc + k, n, g0, sq, max_len, st)) return 0;
         k = end;
     }
     return 1;

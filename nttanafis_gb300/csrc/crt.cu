@@ -188,6 +188,79 @@ __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin)
     return true;
 }
 
+// Carries of a tile of kCrtTile limbs held four per thread, each limb with its
+// (generate, propagate) bits: the thread's composite, an inclusive warp scan, the
+// warps in order, and the tiles before this one by the decoupled look-back
+// (flags: [0] tile counter, [1] error word, [2 + t] state of tile t). Returns the
+// carry into the thread's first limb. Every thread of the CTA calls it (two
+// barriers).
+constexpr int kCrtPer = 4;
+static_assert(kCrtThreads * kCrtPer == kCrtTile, "four limbs per thread");
+
+__device__ __forceinline__ u32 tile_carry_in(const u32 (&gb)[kCrtPer], const u32 (&pb)[kCrtPer], u32 tile,
+                                             u32* flags) {
+    constexpr int NW = kCrtThreads / 32;
+    __shared__ u32 s_wg[NW], s_wp[NW], s_cin;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32 G = gb[0], P = pb[0];
+#pragma unroll
+    for (int c = 1; c < kCrtPer; ++c) {
+        G = gb[c] | (pb[c] & G);
+        P = pb[c] & P;
+    }
+    u32 ig = G, ip = P;
+    warp_scan_gp(ig, ip);
+    u32 xg = __shfl_up_sync(0xffffffffu, ig, 1), xp = __shfl_up_sync(0xffffffffu, ip, 1);
+    if (lane == 0) { xg = 0; xp = 1; }
+    if (lane == 31) { s_wg[warp] = ig; s_wp[warp] = ip; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u32 tg = 0, tp = 1;  // the tile's (generate, propagate) pair
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            tg = s_wg[w] | (s_wp[w] & tg);
+            tp = s_wp[w] & tp;
+        }
+        u32* status = flags + 2;
+        u32 cin = 0;
+        if (tile > 0) {
+            atomicExch(status + tile, kTileAggregate | (tg << 2) | (tp << 3));
+            if (!look_back(status, tile, cin)) {
+                atomicAdd(&g_lookback_timeouts, 1u);
+                atomicOr(&flags[1], 1u);
+                cin = 0;
+            }
+        }
+        atomicExch(status + tile, kTileInclusive | ((tg | (tp & cin)) << 2));
+        s_cin = cin;
+    }
+    __syncthreads();
+    // the tile's carry-in through the earlier warps, then the earlier lanes
+    u32 c = s_cin;
+    for (int w = 0; w < warp; ++w) c = s_wg[w] | (s_wp[w] & c);
+    return xg | (xp & c);
+}
+
+// Adds the carries into a thread's four limbs and stores those below len.
+__device__ __forceinline__ void store_limbs(u64* __restrict__ dst, u64 k0, u64 len, const u64 (&sv)[kCrtPer],
+                                            const u32 (&gb)[kCrtPer], const u32 (&pb)[kCrtPer], u32 c) {
+    u64 out[kCrtPer];
+#pragma unroll
+    for (int i = 0; i < kCrtPer; ++i) {
+        out[i] = sv[i] + c;
+        c = gb[i] | (pb[i] & c);
+    }
+    u64* d = dst + k0;
+    if (k0 + kCrtPer <= len && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+        reinterpret_cast<uint4*>(d)[0] = make_uint4((u32)out[0], (u32)(out[0] >> 32), (u32)out[1], (u32)(out[1] >> 32));
+        reinterpret_cast<uint4*>(d)[1] = make_uint4((u32)out[2], (u32)(out[2] >> 32), (u32)out[3], (u32)(out[3] >> 32));
+    } else {
+#pragma unroll
+        for (int i = 0; i < kCrtPer; ++i)
+            if (k0 + i < len) d[i] = out[i];
+    }
+}
+
 // Tile of kCrtTile output limbs, four per thread: thread t reconstructs the
 // coefficients j0 + 4t .. j0 + 4t + 3 (coefficient k lands at limb k and spans L
 // limbs) and owns the limbs with the same indices. Limb j sums word w of coefficient
@@ -199,9 +272,6 @@ __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin)
 // by the look-back.
 // flags: [0] tile counter, [1] error word, [2 + t] look-back state of tile t; all
 // zero when the kernel starts (the preceding transform kernel clears them).
-constexpr int kCrtPer = 4;
-static_assert(kCrtThreads * kCrtPer == kCrtTile, "four limbs per thread");
-
 // u64 words of a reconstructed coefficient for NP primes below 2^31 (X < 2^(31 NP - 1)).
 __host__ __device__ constexpr int crt_limb_words(int np) {
     return (31 * np - 1 + 63) / 64 < 4 ? (31 * np - 1 + 63) / 64 : 4;
@@ -226,11 +296,10 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
     }
     // Tiles are numbered in the order CTAs start, so a tile only ever waits for
     // tiles whose CTAs are already running.
-    __shared__ u32 s_tile, s_cin;
+    __shared__ u32 s_tile;
     __shared__ u64 s_pre[L][L];              // the L coefficients before the tile
     __shared__ u64 s_edge[NW][NE > 0 ? NE : 1];
     __shared__ u32 s_edge_h[NW];
-    __shared__ u32 s_wg[NW], s_wp[NW];
     if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
     __syncthreads();
     const u32 tile = s_tile;
@@ -356,60 +425,56 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
         pb[c] = s2 == ~0ull ? 1u : 0u;
         hprev = h;
     }
-    // This thread's composite, then an inclusive warp scan of the composites.
-    u32 G = gb[0], P = pb[0];
-#pragma unroll
-    for (int c = 1; c < kCrtPer; ++c) {
-        G = gb[c] | (pb[c] & G);
-        P = pb[c] & P;
-    }
-    u32 ig = G, ip = P;
-    warp_scan_gp(ig, ip);
-    u32 xg = __shfl_up_sync(0xffffffffu, ig, 1), xp = __shfl_up_sync(0xffffffffu, ip, 1);
-    if (lane == 0) { xg = 0; xp = 1; }
-    if (lane == 31) { s_wg[warp] = ig; s_wp[warp] = ip; }
+    store_limbs(dst, k0, out_len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags));
+}
+
+// dst[j] += add[j] for j < len as one big-integer addition (the sum fits in len
+// limbs): four limbs per thread, carries resolved like those of k_crt_mul.
+__global__ void __launch_bounds__(kCrtThreads) k_add_limbs(u64* __restrict__ dst, const u64* __restrict__ add,
+                                                            u64 len, u32* __restrict__ flags) {
+    __shared__ u32 s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        u32 tg = 0, tp = 1;  // the tile's (generate, propagate) pair
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-            tg = s_wg[w] | (s_wp[w] & tg);
-            tp = s_wp[w] & tp;
-        }
-        u32* status = flags + 2;
-        u32 cin = 0;
-        if (tile > 0) {
-            atomicExch(status + tile, kTileAggregate | (tg << 2) | (tp << 3));
-            if (!look_back(status, tile, cin)) {
-                atomicAdd(&g_lookback_timeouts, 1u);
-                atomicOr(&flags[1], 1u);
-                cin = 0;
-            }
-        }
-        atomicExch(status + tile, kTileInclusive | ((tg | (tp & cin)) << 2));
-        s_cin = cin;
-    }
-    __syncthreads();
-    // Carry into this thread's first limb: the tile's carry-in through the earlier
-    // warps, then through the earlier lanes of this warp.
-    u32 c = s_cin;
-    for (int w = 0; w < warp; ++w) c = s_wg[w] | (s_wp[w] & c);
-    c = xg | (xp & c);
-    u64 out[kCrtPer];
+    const u32 tile = s_tile;
+    if ((u64)tile * kCrtTile >= len) return;
+    const u64 k0 = (u64)tile * kCrtTile + (u64)threadIdx.x * kCrtPer;
+    u64 sv[kCrtPer];
+    u32 gb[kCrtPer], pb[kCrtPer];
 #pragma unroll
     for (int i = 0; i < kCrtPer; ++i) {
-        out[i] = sv[i] + c;
-        c = gb[i] | (pb[i] & c);
+        const u64 d = k0 + i < len ? dst[k0 + i] : 0, a = k0 + i < len ? __ldg(add + k0 + i) : 0;
+        const u64 t = d + a;
+        sv[i] = t;
+        gb[i] = t < d ? 1u : 0u;
+        pb[i] = t == ~0ull ? 1u : 0u;
     }
-    u64* d = dst + k0;
-    if (k0 + kCrtPer <= out_len && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
-        reinterpret_cast<uint4*>(d)[0] = make_uint4((u32)out[0], (u32)(out[0] >> 32), (u32)out[1], (u32)(out[1] >> 32));
-        reinterpret_cast<uint4*>(d)[1] = make_uint4((u32)out[2], (u32)(out[2] >> 32), (u32)out[3], (u32)(out[3] >> 32));
-    } else {
-#pragma unroll
-        for (int i = 0; i < kCrtPer; ++i)
-            if (k0 + i < out_len) d[i] = out[i];
-    }
+    store_limbs(dst, k0, len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags));
+}
+
+// Descriptors of blocks first .. first + count - 1 of a split product: block m
+// multiplies a[m*block, m*block + len) by b and lands at limb m*block of dst (m
+// even) or of odd (m odd), so the products of each parity are disjoint.
+__global__ void k_split_descs(ProductDesc* __restrict__ d, u64 first, u64 count, const u64* a, u64 la,
+                              const u64* b, u64 lb, u64 block, u64* dst, u64* odd, uint8_t* arena,
+                              u64 member_bytes, u64 spec_bytes) {
+    const u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const u64 m = first + i, off = m * block;
+    const u64 len = min(block, la - off);
+    uint8_t* base = arena + i * member_bytes;
+    ProductDesc x;
+    x.a = a + off;
+    x.b = b;
+    x.la = len;
+    x.lb = lb;
+    x.spec = reinterpret_cast<u32*>(base);
+    x.conv_len = len + lb - 1;
+    x.dst = ((m & 1) ? odd : dst) + off;
+    x.out_len = len + lb;
+    x.agg = base + spec_bytes;
+    x.square = 0;
+    x.stride = 1;
+    d[i] = x;
 }
 
 // Disjoint blocks: coefficient k fills limbs [k*stride, (k+1)*stride).
@@ -558,6 +623,20 @@ cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u
     const unsigned blocks = (unsigned)((n + kCrtThreads - 1) / kCrtThreads);
     if (sign) k_conv_school<true><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride);
     else k_conv_school<false><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st) {
+    const u64 tiles = (len + kCrtTile - 1) / kCrtTile;
+    k_add_limbs<<<(unsigned)tiles, kCrtThreads, 0, st>>>(dst, add, len, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_descs(ProductDesc* d, u64 first, u64 count, const u64* a, u64 la, const u64* b, u64 lb,
+                               u64 block, u64* dst, u64* odd, uint8_t* arena, u64 member_bytes, u64 spec_bytes,
+                               cudaStream_t st) {
+    k_split_descs<<<(unsigned)((count + 127) / 128), 128, 0, st>>>(d, first, count, a, la, b, lb, block, dst, odd,
+                                                                    arena, member_bytes, spec_bytes);
     return cudaGetLastError();
 }
 

@@ -110,6 +110,14 @@ cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_ti
                                  const CrtParams& cp, cudaStream_t st);
 cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
                                   const CrtParams& cp, cudaStream_t st);
+// dst[0, len) += add[0, len) with carries (flags: carry_flag_words(len), zeroed).
+cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st);
+// Member descriptors of blocks first .. first + count - 1 of a split product
+// (block m of a times b into dst or odd at limb m * block; member m's residues and
+// flags at arena + (m - first) * member_bytes, flags spec_bytes in).
+cudaError_t launch_split_descs(ProductDesc* d, u64 first, u64 count, const u64* a, u64 la, const u64* b, u64 lb,
+                               u64 block, u64* dst, u64* odd, uint8_t* arena, u64 member_bytes, u64 spec_bytes,
+                               cudaStream_t st);
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
                                    int stride, bool sign, cudaStream_t st);
 // Four-step factor tables of one prime and transform length, built on the GPU:

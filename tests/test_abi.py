@@ -38,7 +38,12 @@ def test_mul_plans_reject_like_the_reference(golden):
     for la, lb in [(1, 1), (3, 7), (4, 4), (16, 65), (257, 256)]:
         p = ntt.MulPlan.new(la, lb)
         assert p is not None and p.scratch_len() >= p.sqr_scratch_len()
-    assert ntt.MulPlan.new(2**25, 2) is None  # beyond the GPU transform catalog
+    # beyond one 2^25-point transform: admitted through the block split while the
+    # shorter operand fits a block transform, rejected otherwise
+    p = ntt.MulPlan.new(2**25, 2)
+    assert p is not None and p.blocks > 1
+    assert ntt.MulPlan.new(2**25, 2**25) is None
+    assert ntt.MulPlan.new(2**41, 8) is None
 
 
 def test_conv_strides_match_reference_table(golden):
@@ -76,8 +81,27 @@ def test_conv_plan_matches_oracle_stride_and_output():
 
 
 def test_plans_hold_every_coefficient():
-    # capacity of the chosen primes covers 128 + ceil(log2(min)) bits
-    for la, lb in [(1, 1), (1024, 1024), (2**20, 2**20), (2**20, 131072), (2**24, 2**24), (2**25 - 5, 5)]:
+    # the transform holds the whole product, or one block times the shorter operand
+    for la, lb in [(1, 1), (1024, 1024), (2**20, 2**20), (2**20, 131072), (2**24, 2**24), (2**25 - 5, 5),
+                   (65536, 256), (3000, 1), (2**30, 1000)]:
         p = ntt.MulPlan.new(la, lb)
         assert p is not None, (la, lb)
-        assert (1 << p.log_transform) >= la + lb - 1
+        if p.blocks:
+            assert (1 << p.log_transform) >= p.block_len + min(la, lb) - 1
+            assert p.block_len >= min(la, lb)  # blocks of one parity never overlap
+            assert p.blocks * p.block_len >= max(la, lb) > (p.blocks - 1) * p.block_len
+        else:
+            assert (1 << p.log_transform) >= la + lb - 1
+
+
+def test_block_split_choice():
+    # very unbalanced shapes split; balanced ones and squares never do
+    assert ntt.MulPlan.new(2**20, 1024).blocks > 1
+    assert ntt.MulPlan.new(1024, 2**20).blocks > 1
+    assert ntt.MulPlan.new(2**20, 131072).blocks > 1
+    assert ntt.MulPlan.new(2**20, 2**20).blocks == 0
+    assert ntt.MulPlan.new(4096, 4096).blocks == 0
+    assert ntt.MulPlan.new(300, 40).blocks == 0  # below the smallest block transform
+    split = ntt.MulPlan.new(2**20, 1024)
+    whole_log = (2**20 + 1024 - 1 - 1).bit_length()
+    assert split.log_transform < whole_log

@@ -189,6 +189,55 @@ def test_device_and_plan_scratch_paths(gpu):
     w.close()
 
 
+@pytest.mark.parametrize("la,lb", [(65536, 1024), (1024, 65536), (200000, 3001), (20000, 300), (1 << 20, 1024),
+                                   (1 << 20, 131072)])
+def test_block_split_matches_oracle(ws, gpu, la, lb):
+    # the longer operand in blocks times the shorter one, block sums added with carries
+    assert gpu.MulPlan.new(la, lb).blocks > 1
+    a, b = operand(la, 51), operand(lb, 52)
+    assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b, THREADS)), (la, lb)
+
+
+def test_block_split_all_ones(ws, gpu):
+    # every block sum carries through the whole odd-block addition
+    for la, lb in [(65536, 1000), (70001, 1500)]:
+        assert gpu.MulPlan.new(la, lb).blocks > 1
+        a = np.full(la, MASK, dtype=np.uint64)
+        b = np.full(lb, MASK, dtype=np.uint64)
+        assert np.array_equal(gpu_mul(ws, a, b), all_ones_expected(la, lb))
+
+
+def test_block_split_beyond_one_transform(ws, gpu):
+    # a + b - 1 > 2^25: no single transform holds it, the split does
+    la, lb = (1 << 25) + 12345, 3000
+    plan = gpu.MulPlan.new(la, lb)
+    assert plan is not None and plan.blocks > 1
+    a, b = operand(la, 61), operand(lb, 62)
+    assert fingerprint_ok(a, b, gpu_mul(ws, b, a, extra=1))
+
+
+def test_block_split_plan_scratch(gpu):
+    import torch
+
+    la, lb = 90000, 2000
+    plan = gpu.MulPlan.new(la, lb)
+    assert plan.blocks > 1
+    a, b = operand(la, 71), operand(lb, 72)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    db = torch.from_numpy(b.view(np.int64)).cuda()
+    dst = torch.full((la + lb + 2,), -1, dtype=torch.int64, device="cuda")
+    scratch = torch.empty(plan.scratch_len(), dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    assert plan.mul_device(dst, da, db, scratch, stream)
+    torch.cuda.synchronize()
+    host = dst.cpu().numpy().view(np.uint64)
+    assert np.array_equal(host[:la + lb], oracle.mul(a, b, THREADS)) and np.all(host[la + lb:] == MASK)
+    dst.fill_(-1)
+    assert not plan.mul_device(dst, da, db, scratch[:-1], stream)
+    torch.cuda.synchronize()
+    assert bool((dst == -1).all())
+
+
 def test_no_lookback_timeouts(gpu):
     # every bounded look-back wait of the CRT carry scan completed
     assert gpu.lookback_timeouts() == 0
