@@ -3,13 +3,19 @@
 One step = one exact product of two 1M-limb operands (SplitMix64 seeds 1 and 2
 plus per-set offsets), the workload the reference's headline number is quoted on
 (README.md:28 of the reference: 43.4 ms on one Zen 5 core). Products are
-independent, so N GPUs run N replicas ("scaling": "weak") with no collective on
-the data path; the timed region is bracketed by a barrier and a device sync on
-every rank and the slowest rank's time counts.
+independent: consecutive steps alternate between `--streams` workspaces and CUDA
+streams (default 2), so one product's kernel tails overlap the next one's
+(`config.one_stream_products_per_s` keeps the single-stream figure). N GPUs run N
+replicas ("scaling": "weak") with no collective on the data path; the timed region
+is bracketed by a barrier and a device sync on every rank and the slowest rank's
+time counts.
 
 Printed keys beyond the base contract:
   e2e         the same metric through the host-pointer C ABI call
-              (ntt_mul_workspace_mul) from pinned host buffers, copies included;
+              (ntt_mul_workspace_mul) from pinned host buffers, copies included,
+              made by `--e2e-threads` host threads (default 2) on their own
+              workspaces, so one call's transfers overlap another's kernels
+              (`one_thread_products_per_s` keeps the single-caller figure);
   roofline    algorithmic bytes of one product (operands in, product out, and the
               fused four-step spectrum traffic 8*S with S from the reference
               planner) over the measured device time per product;
@@ -390,19 +396,41 @@ def run_gpu(args) -> None:
     d_a = [torch.from_numpy(a.view(np.int64)).to(dev) for a, _ in host_sets]
     d_b = [torch.from_numpy(b.view(np.int64)).to(dev) for _, b in host_sets]
     d_out = [torch.empty(LA + LB, dtype=torch.int64, device=dev) for _ in range(nsets)]
-    ws = ntt.GpuMulWorkspace()
     plan = ntt.MulPlan.new(LA, LB)
-    assert ws.prepare(plan), ntt.last_error()
-    stream = torch.cuda.Stream(device=dev)
+    # Independent products run on `streams` workspaces and streams (product i on
+    # stream i mod streams), so one product's kernel tails overlap the next one's.
+    nstreams = max(1, args.streams)
+    wss = [ntt.GpuMulWorkspace() for _ in range(nstreams)]
+    for w in wss:
+        assert w.prepare(plan), ntt.last_error()
+    ws = wss[0]
+    streams = [torch.cuda.Stream(device=dev) for _ in range(nstreams)]
+    stream = streams[0]
 
-    def step(i: int) -> None:
+    def step(i: int, n: int = nstreams) -> None:
         k = i % nsets
-        if not ws.mul_device(d_out[k], d_a[k], d_b[k], stream):
+        if not wss[i % n].mul_device(d_out[k], d_a[k], d_b[k], streams[i % n]):
             raise RuntimeError(ntt.last_error())
 
-    with torch.cuda.stream(stream):
-        for i in range(args.warmup):
-            step(i)
+    def timed(steps: int, n: int) -> float:
+        """Device milliseconds of `steps` products spread over n streams."""
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(streams[0])
+        for st in streams[1:n]:
+            st.wait_event(e0)
+        for i in range(steps):
+            step(i, n)
+        for st in streams[1:n]:
+            ev = torch.cuda.Event()
+            ev.record(st)
+            streams[0].wait_event(ev)
+        e1.record(streams[0])
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1)
+
+    for i in range(args.warmup):
+        step(i)
     torch.cuda.synchronize(dev)
 
     # Parity of the timed configuration against exact fingerprints.
@@ -421,34 +449,55 @@ def run_gpu(args) -> None:
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
         t_wall = time.perf_counter()
-        e0.record(stream)
-        for i in range(args.steps):
-            step(i)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
+        dev_ms = timed(args.steps, nstreams)
         t_wall = time.perf_counter() - t_wall
         if world > 1:
             torch.distributed.barrier()
-        dev_ms = e0.elapsed_time(e1)
         launches = ntt.kernel_launches() - launches0
+        one_stream_steps = min(args.steps, 100)
+        one_stream_ms = timed(one_stream_steps, 1) / one_stream_steps
 
-        # End to end through the host-pointer C ABI call, pinned host memory.
-        h_a = torch.from_numpy(host_sets[0][0].view(np.int64)).pin_memory()
-        h_b = torch.from_numpy(host_sets[0][1].view(np.int64)).pin_memory()
-        h_dst = torch.empty(LA + LB, dtype=torch.int64).pin_memory()
-        na, nb, nd = (x.numpy().view(np.uint64) for x in (h_a, h_b, h_dst))
-        e2e_steps = max(3, min(args.steps, 50))
-        for _ in range(2):
-            assert ws.mul(nd, na, nb), ntt.last_error()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            ws.mul(nd, na, nb)
-        e2e_s = time.perf_counter() - t0
-        e2e_ok = fingerprint_ok is None or to_int(nd) % ((1 << 61) - 1) == (A % ((1 << 61) - 1)) * (
-            B % ((1 << 61) - 1)) % ((1 << 61) - 1)
+        # End to end through the host-pointer C ABI call, pinned host memory: each
+        # of `e2e_threads` host threads calls ntt_mul_workspace_mul on its own
+        # workspace (the call blocks until the product is in its pinned buffer).
+        import threading
+
+        nthreads = max(1, args.e2e_threads)
+        e2e_steps = max(3, min(args.steps, 50)) * nthreads
+        bufs = []
+        for t in range(nthreads):
+            h_a = torch.from_numpy(host_sets[t % nsets][0].view(np.int64)).pin_memory()
+            h_b = torch.from_numpy(host_sets[t % nsets][1].view(np.int64)).pin_memory()
+            h_dst = torch.empty(LA + LB, dtype=torch.int64).pin_memory()
+            bufs.append((h_a, h_b, h_dst, *(x.numpy().view(np.uint64) for x in (h_a, h_b, h_dst))))
+        e2e_ws = wss + [ntt.GpuMulWorkspace() for _ in range(nthreads - len(wss))]
+        failures = []
+
+        def caller(t: int, count: int) -> None:
+            na, nb, nd = bufs[t][3:]
+            for _ in range(count):
+                if not e2e_ws[t].mul(nd, na, nb):
+                    failures.append(ntt.last_error())
+
+        def run_e2e(n: int, steps: int) -> float:
+            threads = [threading.Thread(target=caller, args=(t, steps // n + (t < steps % n))) for t in range(n)]
+            t0 = time.perf_counter()
+            for th in threads:
+                th.start()
+            for th in threads:
+                th.join()
+            return time.perf_counter() - t0
+
+        run_e2e(nthreads, 2 * nthreads)
+        e2e_s = run_e2e(nthreads, e2e_steps)
+        e2e_one_s = run_e2e(1, e2e_steps // nthreads) / (e2e_steps // nthreads)
+        assert not failures, failures[:1]
+        e2e_ok = True
+        for t in range(nthreads):
+            At, Bt = to_int(host_sets[t % nsets][0]), to_int(host_sets[t % nsets][1])
+            q = (1 << 61) - 1
+            e2e_ok &= to_int(bufs[t][5]) % q == (At % q) * (Bt % q) % q
 
     max_ms = max_over_ranks(dev_ms, world, dev)
     ms_per_step = max_ms / args.steps
@@ -466,7 +515,7 @@ def run_gpu(args) -> None:
     ms = (ctypes.c_float * (reps * stride))()
     lib.ntt_timing_start(reps * stride)
     for r in range(reps):
-        step(r)
+        step(r, 1)
     got = lib.ntt_timing_stop(ms, reps * stride)
     timed_ok = got == reps * stride - 1
     if timed_ok:
@@ -494,9 +543,11 @@ def run_gpu(args) -> None:
         "vs_baseline": None, "dtype": "u32 modular (NTT primes < 2^31), u64 limbs", "data": "synthetic (SplitMix64)",
         "config": {"workload": WORKLOAD, "la": LA, "lb": LB, "primes": plan.primes,
                    "log_transform": plan.log_transform, "parallelism": f"replicas x{world}",
+                   "streams": nstreams, "one_stream_products_per_s": 1000.0 / one_stream_ms,
                    "l2": f"inputs larger than L2: {nsets} rotating operand pairs ({nsets * per_step_in >> 20} MiB)"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": per_step_in,
                 "d2h_bytes_per_step": 8 * (LA + LB), "api": "ntt_mul_workspace_mul (host pointers, pinned)",
+                "host_threads": nthreads, "one_thread_products_per_s": 1.0 / e2e_one_s,
                 "steps": e2e_steps, "parity_ok": bool(e2e_ok)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -541,6 +592,8 @@ def main() -> None:
     ap.add_argument("--no-served", action="store_true", help="skip the served-configuration section")
     ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration timings")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--streams", type=int, default=2, help="streams (and workspaces) the timed products alternate on")
+    ap.add_argument("--e2e-threads", type=int, default=2, help="host threads making the host-pointer calls")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
