@@ -473,6 +473,20 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
         pp.scale = st.scale;
         pp.fwd = pt.fwd;
         pp.inv = pt.inv;
+        {
+            const u32 gen = generator(p);
+            pp.small_fwd[0] = pp.small_inv[0] = shoup_pair(1, p);
+            for (int h = 1; h < 32; h <<= 1) {
+                const u32 root = powmod(gen, (p - 1) / (2 * (u64)h), p), iroot = invmod(root, p);
+                u32 w = 1, iw = 1;
+                for (int j = 0; j < h; ++j) {
+                    pp.small_fwd[h + j] = shoup_pair(w, p);
+                    pp.small_inv[h + j] = shoup_pair(iw, p);
+                    w = mulmod(w, root, p);
+                    iw = mulmod(iw, iroot, p);
+                }
+            }
+        }
         pp.f4_a = st.f_a;
         pp.f4_b = st.f_b;
         pp.i4_lo = st.i_lo;

@@ -118,6 +118,11 @@ struct PrimeParams {
     const uint2* f4_b;   //                              per column and sweep
     const uint2* i4_lo;  // inverse four-step twiddles: per row, low digit of n2
     const uint2* i4_hi;  //                             per row, high digit, times the scale
+    // Entries 1..31 of the level-major roots (fwd[h + j], inv[h + j] for h < 32), held
+    // in the kernel parameters: register blocks of consecutive points read these
+    // uniform twiddles from the constant cache instead of memory.
+    uint2 small_fwd[32];
+    uint2 small_inv[32];
 };
 
 constexpr int kMaxPrimes = 8;

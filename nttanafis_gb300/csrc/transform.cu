@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant
         u32 x[1][E];
 #pragma unroll
         for (int k = 0; k < E; ++k) x[0][k] = base[k];
-        dif_levels<A, 5, 1, 1>(x, pp.fwd, pp.p);
+        dif_levels<A, 5, 1, 1>(x, pp.small_fwd, pp.p);
         const uint2 fb = __ldg(pp.f4_b + ((size_t)col << 5) + (__brev((u32)blk) >> 27));
         const uint2* fac = fa + c * (E + 1);
         u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + ((u64)(blk * E) << log_c) + col;
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant
         u32 x[1][E];
 #pragma unroll
         for (int k = 0; k < E; ++k) x[0][k] = __ldcs(q + ((u64)k << log_c));
-        dit_levels<A, 5, 1, 1>(x, pp.inv, pp.p);
+        dit_levels<A, 5, 1, 1>(x, pp.small_inv, pp.p);
         u32* base = sm + c * VS + 33 * blk;
 #pragma unroll
         for (int k = 0; k < E; ++k) base[k] = x[0][k];
@@ -430,11 +430,11 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
             for (int q = 0; q < NV; ++q)
 #pragma unroll
                 for (int k = 0; k < E; ++k) x[q][k] = base[q * VS + k];
-            dif_levels<A, RBL, 1, NV>(x, pp.fwd, pp.p);
+            dif_levels<A, RBL, 1, NV>(x, pp.small_fwd, pp.p);
 #pragma unroll
             for (int k = 0; k < E; ++k) x[0][k] = A::pointwise(x[0][k], x[NV - 1][k], pp.p, pp.pni);
             u32(&y)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
-            dit_levels<A, RBL, 1, 1>(y, pp.inv, pp.p);
+            dit_levels<A, RBL, 1, 1>(y, pp.small_inv, pp.p);
 #pragma unroll
             for (int k = 0; k < E; ++k) base[k] = x[0][k];
         }
