@@ -13,7 +13,7 @@ time counts.
 Printed keys beyond the base contract:
   e2e         the same metric through the host-pointer C ABI call
               (ntt_mul_workspace_mul) from pinned host buffers, copies included,
-              made by `--e2e-threads` host threads (default 2) on their own
+              made by `--e2e-threads` host threads (default 4) on their own
               workspaces, so one call's transfers overlap another's kernels
               (`one_thread_products_per_s` keeps the single-caller figure);
   roofline    algorithmic bytes of one product (operands in, product out, and the
@@ -593,7 +593,7 @@ def main() -> None:
     ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration timings")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--streams", type=int, default=2, help="streams (and workspaces) the timed products alternate on")
-    ap.add_argument("--e2e-threads", type=int, default=2, help="host threads making the host-pointer calls")
+    ap.add_argument("--e2e-threads", type=int, default=4, help="host threads making the host-pointer calls")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -760,16 +760,29 @@ static void* mapped_host_pointer(void* p) {
     return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
 }
 
+// Host-pointer calls in flight in this process.
+static std::atomic<int> g_host_calls{0};
+
 // Runs a host-pointer call. The operands are copied in (b on a second stream,
 // overlapping a's column pass); the result is written straight into dst when dst
-// is page-locked host memory the GPU can address, and copied out otherwise. One
+// is page-locked host memory the GPU can address and no other host-pointer call is
+// in flight, and copied out otherwise. One
 // synchronisation at the end: every check runs before the first write, and a
 // failed kernel stops the stream before the copy-out.
 template <class W>
 static bool run_host(W* ws, const Geom& g, bool square, u64* dst, const u64* a, const u64* b) {
     const size_t out_bytes = g.out_len * sizeof(u64);
-    // a split product adds into its destination: keep that in device memory
-    u64* direct = g.split() ? nullptr : (u64*)mapped_host_pointer(dst);
+    // The CRT kernel writes straight into page-locked dst when this is the only
+    // host-pointer call in flight (lowest latency). With others in flight the copy
+    // engine moves the result instead, so the SMs stay free for their kernels while
+    // the bytes cross the host link. A split product adds into its destination:
+    // that stays in device memory.
+    struct InFlight {
+        InFlight() { ++g_host_calls; }
+        ~InFlight() { --g_host_calls; }
+    } in_flight;
+    const bool alone = g_host_calls.load() == 1;
+    u64* direct = g.split() || !alone ? nullptr : (u64*)mapped_host_pointer(dst);
     if (!ws->a.ensure(g.la * 8) || (!square && !ws->b.ensure(g.lb * 8)) || (!direct && !ws->out.ensure(out_bytes)) ||
         !ws->scratch.ensure(g.scratch_bytes(square)))
         return false;
