@@ -58,6 +58,26 @@ struct LazyArith {
     static __device__ __forceinline__ u32 mulc(u32 x, uint2 w, u32 p) {
         return shoup_mul(x, w.x, w.y, p);
     }
+    // Last forward level (twiddle 1) left open for a following product: x, y in
+    // [0, 2p) -> [0, 4p), without the reductions.
+    static __device__ __forceinline__ void dif_open(u32& x, u32& y, u32 p) {
+        const u32 s = x + y;
+        y = x - y + (p << 1);
+        x = s;
+    }
+    // First inverse level (twiddle 1): x, y in [0, 4p) -> [0, 4p), no product.
+    static __device__ __forceinline__ void dit_unit(u32& x, u32& y, u32 p) {
+        const u32 p2 = p << 1;
+        const u32 a = sub_if_ge(x, p2), t = sub_if_ge(y, p2);
+        x = a + t;
+        y = a - t + p2;
+    }
+    // The same for x, y already in [0, 2p) (the residues the row pass writes).
+    static __device__ __forceinline__ void dit_unit_2p(u32& x, u32& y, u32 p) {
+        const u32 s = x + y;
+        y = x - y + (p << 1);
+        x = s;
+    }
     // Pointwise product of two forward-domain values -> inverse domain, times 2^-32.
     static __device__ __forceinline__ u32 pointwise(u32 a, u32 b, u32 p, u32 pni) {
         return mont_mul(a, b, p, pni);
@@ -93,6 +113,19 @@ struct WideArith {
     static __device__ __forceinline__ u32 mulc(u32 x, uint2 w, u32 p) {
         return sub_if_ge(shoup_mul(x, w.x, w.y, p), p);
     }
+    // x, y in [0, p) -> [0, 2p), without the reductions.
+    static __device__ __forceinline__ void dif_open(u32& x, u32& y, u32 p) {
+        const u32 s = x + y;
+        y = x - y + p;
+        x = s;
+    }
+    // Twiddle-1 inverse level on canonical values.
+    static __device__ __forceinline__ void dit_unit(u32& x, u32& y, u32 p) {
+        const u32 s = x + y, d = x - y + p;
+        x = sub_if_ge(s, p);
+        y = sub_if_ge(d, p);
+    }
+    static __device__ __forceinline__ void dit_unit_2p(u32& x, u32& y, u32 p) { dit_unit(x, y, p); }
     static __device__ __forceinline__ u32 pointwise(u32 a, u32 b, u32 p, u32 pni) {
         return sub_if_ge(mont_mul(a, b, p, pni), p);
     }

@@ -48,11 +48,23 @@ __host__ __device__ constexpr int vectors_per_block() {
 // twiddle of butterfly c at the level of half-size h = 2^(RB-1-t) * H is
 // twb[h + c * H], twb = table + (first point mod H). With HZ the upper half of
 // every block is zero, so the first level only multiplies: (x, 0) -> (x, x*w).
-template <class A, int RB, int H, int VP, bool HZ = false>
+//
+// With OPEN (blocks of consecutive points, H = 1) the last level, whose twiddle is
+// 1, is left open: its pairs come out as (x + y, x - y + 2p) unreduced (A::dif_open)
+// for a caller that multiplies them next.
+template <class A, int RB, int H, int VP, bool HZ = false, bool OPEN = false>
 __device__ __forceinline__ void dif_levels(u32 (&x)[VP][1 << RB], const uint2* __restrict__ twb, u32 p) {
     constexpr int E = 1 << RB;
+    static_assert(!OPEN || H == 1, "an open last level has twiddle 1 only for consecutive points");
 #pragma unroll
     for (int t = 0; t < RB; ++t) {
+        if (OPEN && t == RB - 1) {
+#pragma unroll
+            for (int q = 0; q < VP; ++q)
+#pragma unroll
+                for (int b = 0; b < E; b += 2) A::dif_open(x[q][b], x[q][b + 1], p);
+            break;
+        }
         const int half = E >> (t + 1);
 #pragma unroll
         for (int c = 0; c < half; ++c) {
@@ -69,13 +81,26 @@ __device__ __forceinline__ void dif_levels(u32 (&x)[VP][1 << RB], const uint2* _
     }
 }
 
-// RB inverse levels on VP register blocks of 2^RB points spaced H apart.
-template <class A, int RB, int H, int VP>
+// RB inverse levels on VP register blocks of 2^RB points spaced H apart. UNIT
+// (H = 1: the first level's twiddle is 1) runs that level without products:
+// 1 for inputs in [0, 4p) (A::dit_unit), 2 for inputs in [0, 2p) (A::dit_unit_2p).
+template <class A, int RB, int H, int VP, int UNIT = 0>
 __device__ __forceinline__ void dit_levels(u32 (&x)[VP][1 << RB], const uint2* __restrict__ twb, u32 p) {
     constexpr int E = 1 << RB;
+    static_assert(UNIT == 0 || H == 1, "a product-free first level needs consecutive points");
 #pragma unroll
     for (int t = 0; t < RB; ++t) {
         const int dist = 1 << t;
+        if (UNIT && t == 0) {
+#pragma unroll
+            for (int q = 0; q < VP; ++q)
+#pragma unroll
+                for (int b = 0; b < E; b += 2) {
+                    if (UNIT == 2) A::dit_unit_2p(x[q][b], x[q][b + 1], p);
+                    else A::dit_unit(x[q][b], x[q][b + 1], p);
+                }
+            continue;
+        }
 #pragma unroll
         for (int c = 0; c < dist; ++c) {
             const uint2 w = twb[(H << t) + c * H];

@@ -302,7 +302,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant
         u32 x[1][E];
 #pragma unroll
         for (int k = 0; k < E; ++k) x[0][k] = base[k];
-        dif_levels<A, 5, 1, 1>(x, pp.small_fwd, pp.p);
+        // the last level (twiddle 1) stays open: its outputs go straight into the
+        // product by the four-step factor, which accepts them unreduced
+        dif_levels<A, 5, 1, 1, false, true>(x, pp.small_fwd, pp.p);
         const uint2 fb = __ldg(pp.f4_b + ((size_t)col << 5) + (__brev((u32)blk) >> 27));
         const uint2* fac = fa + c * (E + 1);
         u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + ((u64)(blk * E) << log_c) + col;
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant
         u32 x[1][E];
 #pragma unroll
         for (int k = 0; k < E; ++k) x[0][k] = __ldcs(q + ((u64)k << log_c));
-        dit_levels<A, 5, 1, 1>(x, pp.small_inv, pp.p);
+        dit_levels<A, 5, 1, 1, 2>(x, pp.small_inv, pp.p);  // the row pass wrote [0, 2p)
         u32* base = sm + c * VS + 33 * blk;
 #pragma unroll
         for (int k = 0; k < E; ++k) base[k] = x[0][k];
@@ -430,11 +432,21 @@ __global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) 
             for (int q = 0; q < NV; ++q)
 #pragma unroll
                 for (int k = 0; k < E; ++k) x[q][k] = base[q * VS + k];
-            dif_levels<A, RBL, 1, NV>(x, pp.small_fwd, pp.p);
+            // a's last level stays open (the Montgomery product takes one factor
+            // below 4p), b's is reduced; the product is below 3p, so the first
+            // inverse level (twiddle 1) needs no products either
+            if constexpr (NV == 2) {
+                u32(&xa)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
+                u32(&xb)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[1]);
+                dif_levels<A, RBL, 1, 1, false, true>(xa, pp.small_fwd, pp.p);
+                dif_levels<A, RBL, 1, 1>(xb, pp.small_fwd, pp.p);
+            } else {
+                dif_levels<A, RBL, 1, NV>(x, pp.small_fwd, pp.p);
+            }
 #pragma unroll
             for (int k = 0; k < E; ++k) x[0][k] = A::pointwise(x[0][k], x[NV - 1][k], pp.p, pp.pni);
             u32(&y)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
-            dit_levels<A, RBL, 1, 1>(y, pp.small_inv, pp.p);
+            dit_levels<A, RBL, 1, 1, 1>(y, pp.small_inv, pp.p);
 #pragma unroll
             for (int k = 0; k < E; ++k) base[k] = x[0][k];
         }
