@@ -203,6 +203,41 @@ uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const uint64_t* 
 int ntt_timing_start(int count);
 int ntt_timing_stop(float* ms, int capacity);
 
+/* ---------------------------------------------------------------------------
+ * Batched modular arithmetic in 50-bit prime fields (the reference's PrimeField
+ * and CrtPair, src/field/prime_field.rs), on device arrays of residues (uint64_t,
+ * canonical 0 <= r < p; residues of another field give unspecified values). A
+ * field is named by its modulus, a prime 2^49 < p < 2^50; every call checks it
+ * (returns 0 otherwise). Calls enqueue on `stream` and return without waiting.
+ */
+
+/* 1 when `modulus` is a prime in (2^49, 2^50): PrimeField::new, prime_field.rs:99. */
+int ntt_field_check(uint64_t modulus);
+/* Largest admitted prime below min(bound, 2^50), or 0: PrimeField::below, :118. */
+uint64_t ntt_field_below(uint64_t bound);
+/* The transform's catalog moduli in reconstruction order (writes at most
+ * `capacity`, returns 8): PrimeField::catalog, :131. */
+size_t ntt_field_catalog(uint64_t* out, size_t capacity);
+/* out[i] = a[i] op b[i]; op 0 add (:205), 1 sub (:215), 2 mul (:232). */
+uint8_t ntt_field_binary_device(uint64_t modulus, int op, uint64_t* d_out, const uint64_t* d_a,
+                                const uint64_t* d_b, size_t n, void* stream);
+/* out[i] = op(a[i]); op 0 neg (:225), 1 pow with `exponent` (:249, 0^0 = 1),
+ * 2 inv (:271; zero gives 0 and, with d_mask, mask 0), 3 signed representative
+ * as int64 bits (:193), 4 reduce of int64 bits (:158), 5 reduce of uint64 (:173). */
+uint8_t ntt_field_unary_device(uint64_t modulus, int op, uint64_t* d_out, const uint64_t* d_a, size_t n,
+                               uint64_t exponent, uint8_t* d_mask, void* stream);
+/* target[i] = factor * target[i] (scale, :304), or with d_source
+ * target[i] -= factor * source[i] (mul_sub, :296). factor < modulus. */
+uint8_t ntt_field_scale_device(uint64_t modulus, uint64_t* d_target, const uint64_t* d_source, size_t n,
+                               uint64_t factor, void* stream);
+/* out[j] = sum_i coeffs[i] * points[j]^i for every point (evaluate, :313). */
+uint8_t ntt_field_evaluate_device(uint64_t modulus, uint64_t* d_out, const uint64_t* d_coeffs, size_t n_coeffs,
+                                  const uint64_t* d_points, size_t n_points, void* stream);
+/* CrtPair::combine (:428) of two distinct fields: out[2i], out[2i+1] = low and
+ * high words of the int128 in -(M-1)/2..(M-1)/2 congruent to first[i] and second[i]. */
+uint8_t ntt_crt_pair_combine_device(uint64_t first, uint64_t second, int64_t* d_out, const uint64_t* d_first,
+                                    const uint64_t* d_second, size_t n, void* stream);
+
 /* Look-back waits of the CRT carry scan that gave up since the library was loaded
  * (each wait is bounded; a nonzero count means a result may be wrong). Synchronizes
  * the device. */

@@ -15,6 +15,7 @@ from .api import (  # noqa: F401
     lookback_timeouts,
     library,
 )
+from .field import CrtPair, PrimeField  # noqa: F401
 from .operands import operand  # noqa: F401
 
 __version__ = "0.1.0"

@@ -102,6 +102,23 @@ _SIGNATURES = [
     ("ntt_timing_start", ctypes.c_int, [ctypes.c_int]),
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_lookback_timeouts", ctypes.c_uint32, []),
+    ("ntt_field_check", ctypes.c_int, [ctypes.c_uint64]),
+    ("ntt_field_below", ctypes.c_uint64, [ctypes.c_uint64]),
+    ("ntt_field_catalog", ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_size_t]),
+    ("ntt_field_binary_device", ctypes.c_uint8,
+     [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
+    ("ntt_field_unary_device", ctypes.c_uint8,
+     [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64,
+      ctypes.c_void_p, ctypes.c_void_p]),
+    ("ntt_field_scale_device", ctypes.c_uint8,
+     [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_void_p]),
+    ("ntt_field_evaluate_device", ctypes.c_uint8,
+     [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
+    ("ntt_crt_pair_combine_device", ctypes.c_uint8,
+     [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+      ctypes.c_void_p]),
     ("ntt_last_error", ctypes.c_char_p, []),
     ("ntt_kernel_launches", ctypes.c_uint64, []),
     ("ntt_version", ctypes.c_char_p, []),
