@@ -241,3 +241,52 @@ def test_block_split_plan_scratch(gpu):
 def test_no_lookback_timeouts(gpu):
     # every bounded look-back wait of the CRT carry scan completed
     assert gpu.lookback_timeouts() == 0
+
+
+def test_concurrent_host_calls_and_streams(gpu):
+    # several host threads on their own workspaces (the copy-out result path that
+    # concurrent host-pointer calls take) and products on two streams at once
+    import threading
+
+    import torch
+
+    shapes = [(70000, 50000), (1 << 16, 1 << 16), (30000, 3), (4096, 4096), (200000, 3001), (1 << 20, 1 << 20)]
+    expected = {s: oracle.mul(operand(s[0], 81 + i), operand(s[1], 91 + i), THREADS) for i, s in enumerate(shapes)}
+    errors = []
+
+    def worker(t):
+        w = gpu.GpuMulWorkspace()
+        try:
+            for r in range(3):
+                for i, (la, lb) in enumerate(shapes[t::2]):
+                    k = shapes.index((la, lb))
+                    a, b = operand(la, 81 + k), operand(lb, 91 + k)
+                    dst = torch.empty(la + lb, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+                    if not w.mul(dst, a, b) or not np.array_equal(dst, expected[(la, lb)]):
+                        errors.append((t, la, lb))
+        finally:
+            w.close()
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    # device calls alternating on two streams with two workspaces
+    wss = [gpu.GpuMulWorkspace() for _ in range(2)]
+    sts = [torch.cuda.Stream() for _ in range(2)]
+    outs = []
+    for i, (la, lb) in enumerate(shapes * 2):
+        k = shapes.index((la, lb))
+        da = torch.from_numpy(operand(la, 81 + k).view(np.int64)).cuda()
+        db = torch.from_numpy(operand(lb, 91 + k).view(np.int64)).cuda()
+        out = torch.empty(la + lb, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()
+        assert wss[i % 2].mul_device(out, da, db, sts[i % 2])
+        outs.append(((la, lb), out, da, db))
+    torch.cuda.synchronize()
+    for (la, lb), out, _, _ in outs:
+        assert np.array_equal(out.cpu().numpy().view(np.uint64), expected[(la, lb)]), (la, lb)
+    for w in wss:
+        w.close()
