@@ -31,21 +31,18 @@ constexpr int kThreads = kColThreads;
 #ifndef NTT_COLS_MINB
 #define NTT_COLS_MINB 0
 #endif
-#ifndef NTT_ROWS_MINB
-#define NTT_ROWS_MINB 0
-#endif
 #if NTT_COLS_MINB > 0
 #define NTT_COLS_BOUNDS __launch_bounds__(kThreads, NTT_COLS_MINB)
 #else
 #define NTT_COLS_BOUNDS __launch_bounds__(kThreads)
 #endif
-#if NTT_ROWS_MINB > 0
-#define NTT_ROWS_BOUNDS __launch_bounds__(kRowThreads, NTT_ROWS_MINB)
-#else
-#define NTT_ROWS_BOUNDS __launch_bounds__(kRowThreads)
-#endif
-// Threads of a row-pass CTA.
-constexpr int kRowThreads = NTT_ROW_THREADS;
+// Threads of a row-pass CTA: at least NTT_ROW_THREADS, and one per register block
+// of the first pass (C / 16) up to 512, so that no pass loops twice over its
+// blocks (two iterations made the compiler hold both in registers).
+__host__ __device__ constexpr int row_threads(int log_c) {
+    return (1 << (log_c - 4)) > NTT_ROW_THREADS ? ((1 << (log_c - 4)) < 512 ? (1 << (log_c - 4)) : 512)
+                                                : NTT_ROW_THREADS;
+}
 
 // log2 of the columns one CTA of a column pass owns: 8 columns, so a row segment
 // is one 32-byte sector of u32 residues (two of u64 limbs).
@@ -355,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant
 // Rows per CTA of the row pass: enough that every thread owns a register block of
 // the first pass (2^(log_c - kMaxRB) blocks per row).
 __host__ __device__ constexpr int row_log_rpc(int log_c) {
-    return log_c - kMaxRB >= ilog2(kRowThreads) ? 0 : ilog2(kRowThreads) - (log_c - kMaxRB);
+    return log_c - kMaxRB >= ilog2(row_threads(log_c)) ? 0 : ilog2(row_threads(log_c)) - (log_c - kMaxRB);
 }
 
 // Row pass: forward rows of a (and b), pointwise product, inverse rows, inverse
@@ -368,7 +365,8 @@ __host__ __device__ constexpr int row_log_rpc(int log_c) {
 // work on blocks of 2^RBL consecutive points), and the last inverse pass applies
 // the twiddle and writes global memory.
 template <class A, bool SQUARE, int LOG_C>
-__global__ void NTT_ROWS_BOUNDS k_rows(const __grid_constant__ TransformArgs g) {
+__global__ void __launch_bounds__(row_threads(LOG_C)) k_rows(const __grid_constant__ TransformArgs g) {
+    constexpr int kRowThreads = row_threads(LOG_C);
     extern __shared__ u32 sm[];
     constexpr int C = 1 << LOG_C;
     constexpr int VS = padded_len(C);
@@ -672,7 +670,7 @@ static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st,
     if (init) return opt_in(k, NTT_ROWS_CARVEOUT);
     const dim3 grid(1u << (g.log_r - row_log_rpc(L)), g.np, g.batch ? g.count : 1);
     const size_t smem = row_smem(L, square);
-    k<<<grid, kRowThreads, smem, st>>>(g);
+    k<<<grid, row_threads(L), smem, st>>>(g);
     return cudaGetLastError();
 }
 
