@@ -375,6 +375,40 @@ def served_section(dev, count: int = 400, rates=(2000.0, 20000.0), budget_gb: fl
     return out
 
 
+def field_section(dev, n: int = 1 << 26, reps: int = 20) -> dict:
+    """Batched PrimeField products (the catalog's first field) over n residues, with
+    each product method: elements/s of out = a * b, inputs resident."""
+    import torch
+
+    import nttanafis_gb300 as ntt
+    from nttanafis_gb300.field import mul_method
+
+    f = next(ntt.PrimeField.catalog())
+    gen = torch.Generator(device=dev).manual_seed(11)
+    a = torch.randint(0, f.modulus, (n,), device=dev, generator=gen)
+    b = torch.randint(0, f.modulus, (n,), device=dev, generator=gen)
+    outs = {}
+    result = {"workload": f"out = a * b mod p over {n} residues of p = {f.modulus}"}
+    previous = mul_method()
+    for name, m in (("barrett", 0), ("fp64", 1)):
+        mul_method(m)
+        out = torch.empty_like(a)
+        f.mul(out, a, b)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            f.mul(out, a, b)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        result[name] = {"elements_per_s": n / (ms / 1000.0), "ms": ms, "gb_per_s": 24 * n / (ms / 1000.0) / 1e9}
+        outs[name] = out
+    mul_method(previous)
+    result["bit_identical"] = bool(torch.equal(outs["barrett"], outs["fp64"]))
+    return result
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -565,6 +599,8 @@ def run_gpu(args) -> None:
         line["batched"] = batched_section(dev, stream)
     if rank == 0 and not args.no_served:
         line["served"] = served_section(dev)
+    if rank == 0 and not args.no_configs:
+        line["field"] = field_section(dev)
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
         multi = cpu_sample(cores, seconds=args.cpu_seconds)

@@ -213,6 +213,11 @@ int ntt_timing_stop(float* ms, int capacity);
 
 /* 1 when `modulus` is a prime in (2^49, 2^50): PrimeField::new, prime_field.rs:99. */
 int ntt_field_check(uint64_t modulus);
+/* Selects how the calls below multiply two residues (process-wide; returns the
+ * previous choice): 1 the reference's FP64 quotient estimate (prime_field.rs:232),
+ * 0 Barrett on 64-bit integers; any other value only reports. Both are exact. No
+ * reference counterpart: it exists to measure and test the two methods. */
+int ntt_field_mul_method(int method);
 /* Largest admitted prime below min(bound, 2^50), or 0: PrimeField::below, :118. */
 uint64_t ntt_field_below(uint64_t bound);
 /* The transform's catalog moduli in reconstruction order (writes at most

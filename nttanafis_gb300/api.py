@@ -103,6 +103,7 @@ _SIGNATURES = [
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_lookback_timeouts", ctypes.c_uint32, []),
     ("ntt_field_check", ctypes.c_int, [ctypes.c_uint64]),
+    ("ntt_field_mul_method", ctypes.c_int, [ctypes.c_int]),
     ("ntt_field_below", ctypes.c_uint64, [ctypes.c_uint64]),
     ("ntt_field_catalog", ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_size_t]),
     ("ntt_field_binary_device", ctypes.c_uint8,

@@ -18,6 +18,12 @@ _ADD, _SUB, _MUL = 0, 1, 2
 _NEG, _POW, _INV, _SIGNED, _REDUCE, _REDUCE_U64 = 0, 1, 2, 3, 4, 5
 
 
+def mul_method(method: Optional[int] = None) -> int:
+    """The product method of the field calls: 1 FP64 quotient estimate (the
+    reference's), 0 Barrett; sets it when given and returns the previous one."""
+    return int(library().ntt_field_mul_method(-1 if method is None else method))
+
+
 def _check(ok: int) -> None:
     if not ok:
         raise RuntimeError(last_error())

@@ -60,8 +60,18 @@ def test_known_answers():
     assert got == vals
 
 
+@pytest.fixture(params=[0, 1], ids=["barrett", "fp64"])
+def method(request):
+    # both product methods (Barrett on integers, the reference's FP64 estimate)
+    from nttanafis_gb300.field import mul_method
+
+    previous = mul_method(request.param)
+    yield request.param
+    mul_method(previous)
+
+
 @pytest.mark.parametrize("index", range(9))
-def test_arithmetic_matches_integers(index):
+def test_arithmetic_matches_integers(index, method):
     f = fields()[index]
     p = f.modulus
     rng = np.random.default_rng(100 + index)
@@ -101,7 +111,7 @@ def test_arithmetic_matches_integers(index):
 
 
 @pytest.mark.parametrize("index", [0, 3, 8])
-def test_slice_kernels(index):
+def test_slice_kernels(index, method):
     f = fields()[index]
     p = f.modulus
     rng = np.random.default_rng(7 + index)
