@@ -335,11 +335,16 @@ def served_section(dev, count: int = 400, rates=(2000.0, 20000.0), budget_gb: fl
     out = {"workload": f"{count} requests per rate; mul/sqr 192..4194304 limbs, conv 1024..4194304 coefficients "
                        "(16-bit, 32-bit unsigned, 32-bit signed)", "budget_bytes": int(budget_gb * 2**30),
            "slots": slots, "rates": []}
-    warm = served_stream(32, 1e9, seed=99, max_limbs=1 << 16)
+    # Warm-up over the whole size range: root tables and batch arenas reach their
+    # working sizes before the timed streams (a server starts warm).
+    warm = served_stream(count, 1e9, seed=99)
+    ex.preload(warm)
     serve(warm, ex, int(budget_gb * 2**30), slots)
     torch.cuda.synchronize(dev)
     for rate in rates:
         stream = served_stream(count, rate, seed=7)
+        ex.preload(stream)
+        torch.cuda.synchronize(dev)
         stats = serve(stream, ex, int(budget_gb * 2**30), slots)
         torch.cuda.synchronize(dev)
         finished = stats.pop("finished")
@@ -598,7 +603,7 @@ def run_gpu(args) -> None:
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_section(dev, stream)
     if rank == 0 and not args.no_served:
-        line["served"] = served_section(dev)
+        line["served"] = served_section(dev, slots=args.served_slots)
     if rank == 0 and not args.no_configs:
         line["field"] = field_section(dev)
     if rank == 0 and not args.no_cpu:
@@ -630,6 +635,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--streams", type=int, default=2, help="streams (and workspaces) the timed products alternate on")
     ap.add_argument("--e2e-threads", type=int, default=4, help="host threads making the host-pointer calls")
+    ap.add_argument("--served-slots", type=int, default=4, help="batches in flight in the served section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

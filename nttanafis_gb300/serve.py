@@ -196,12 +196,24 @@ class GpuExecutor:
         scratch = plan.sqr_scratch_len() if item.kind == "sqr" else plan.scratch_len()
         return 8 * (scratch + item.la + item.lb)
 
-    def prepare(self, item):
+    def _make(self, item):
         from .api import Request
 
         a, b = self.operands(item)
         dst = self.torch.empty(item.out_len(), dtype=self.torch.int64, device=self.device)
         return Request(dst, a, b, "conv" if item.kind == "conv" else "mul", item.max_a, item.max_a, item.signed)
+
+    def preload(self, items) -> None:
+        """Allocates the result buffers of `items` ahead of time (a server draws
+        them from a pool; allocating on arrival would put the allocator's device
+        synchronisations inside the loop)."""
+        self._pre = {id(it): self._make(it) for it in items}
+
+    def prepare(self, item):
+        pre = getattr(self, "_pre", None)
+        if pre is not None and id(item) in pre:
+            return pre.pop(id(item))
+        return self._make(item)
 
     def launch(self, slot: Slot, payloads):
         from .api import last_error
