@@ -520,6 +520,10 @@ static bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq
     ta.log_t = g0.log_t;
     ta.wide = g0.wide;
     const bool sign = g0.sign != 0;
+    if (!g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
+        g_launches += 1;
+        return cuda_ok(launch_small_fused(ta, cp, sq, st), "batched fused product launch");
+    }
     if (g0.log_t <= kMaxBlockLog) {
         g_launches += 1;
         if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return false;
@@ -610,6 +614,16 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         ta.flag_words = (u32)carry_flag_words(g.out_len);
     }
     const bool sign = g.sign != 0;
+    if (!g.conv && g.log_t <= kFusedMaxLog && g.np == kFusedPrimes && !g.wide) {
+        // the whole product in one cluster launch
+        if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
+        ta.dst = d_dst;
+        ta.out_len = g.out_len;
+        g_launches += 1;
+        const bool ok = cuda_ok(launch_small_fused(ta, cp, square, st), "fused product launch");
+        mark(st);
+        return ok;
+    }
     if (g.log_t <= kMaxBlockLog) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         g_launches += 1;

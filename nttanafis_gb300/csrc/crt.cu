@@ -14,76 +14,10 @@
 // resolves the tile's carry-in with a decoupled look-back over the earlier tiles'
 // published (generate, propagate) pairs, so the limbs are written once, final.
 // Every look-back wait is bounded; a wait that gives up is counted and flagged.
+#include "crt.cuh"
 #include "launch.h"
 
 namespace ntt {
-
-constexpr int kCrtThreads = kCrtTile / 4;
-
-// Reconstructs X from its residues r_i: returns the NP + 1 u32 words (two's
-// complement) of X = S - q*P, S = sum_i y_i*(P/p_i), y_i = r_i*(P/p_i)^-1 mod p_i,
-// q rounded from sum_i y_i/p_i. Unsigned: 0 <= X < P/2. Signed: |X| <= P/4.
-template <int NP>
-__device__ __forceinline__ void crt_words(const u32 (&r)[NP], const CrtParams& cp, u32 (&x)[NP + 1]) {
-    u32 y[NP];
-    float f = 0.0f;
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const u32 p = cp.p[i];
-        u32 v = shoup_mul(r[i], cp.inv[i].x, cp.inv[i].y, p);
-        v = sub_if_ge(v, p);
-        y[i] = v;
-        f = fmaf((float)v, cp.pinv[i], f);
-    }
-    constexpr int MW = NP > 1 ? NP - 1 : 1;  // words of P/p_i
-    // S = sum_i y_i * M_i in NP + 1 words (the top word stays zero), by carry
-    // chains: the low halves of y_i * M_i[w] into word w, the high halves into w+1.
-    u32 S[NP + 1];
-#pragma unroll
-    for (int w = 0; w <= NP; ++w) S[w] = 0;
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const u32 yi = y[i];
-        asm volatile("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(S[0]) : "r"(yi), "r"(cp.M[i][0]));
-#pragma unroll
-        for (int w = 1; w < MW; ++w)
-            asm volatile("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(S[w]) : "r"(yi), "r"(cp.M[i][w]));
-#pragma unroll
-        for (int w = MW; w <= NP; ++w) asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(S[w]));
-        asm volatile("mad.hi.cc.u32 %0, %1, %2, %0;" : "+r"(S[1]) : "r"(yi), "r"(cp.M[i][0]));
-#pragma unroll
-        for (int w = 2; w <= MW; ++w)
-            asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(S[w]) : "r"(yi), "r"(cp.M[i][w - 1]));
-#pragma unroll
-        for (int w = MW + 1; w <= NP; ++w) asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(S[w]));
-    }
-    // X = S - q*P in NP + 1 words; the top word is the sign (0 or all ones).
-    const u32 q = (u32)(f + cp.bias);
-    u32 U[NP + 1];
-#pragma unroll
-    for (int w = 0; w < NP; ++w) U[w] = q * cp.P[w];
-    U[NP] = 0;
-    asm volatile("mad.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[1]) : "r"(q), "r"(cp.P[0]));
-#pragma unroll
-    for (int w = 2; w <= NP; ++w)
-        asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[w]) : "r"(q), "r"(cp.P[w - 1]));
-    asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(x[0]) : "r"(S[0]), "r"(U[0]));
-#pragma unroll
-    for (int w = 1; w <= NP; ++w) asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(x[w]) : "r"(S[w]), "r"(U[w]));
-}
-
-// The first W u64 words of X (sign-filled above its NP + 1 u32 words).
-template <int NP, int W>
-__device__ __forceinline__ void pack_words(const u32 (&x)[NP + 1], u64 (&out)[W]) {
-    const u64 fill = x[NP] ? ~0ull : 0ull;
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-        const int lo = 2 * w, hi = 2 * w + 1;
-        const u64 l = lo <= NP ? (u64)x[lo] : fill & 0xffffffffull;
-        const u64 h = hi <= NP ? (u64)x[hi] : fill & 0xffffffffull;
-        out[w] = l | (h << 32);
-    }
-}
 
 // Coefficient k of a residue array [prime][T] as four u64 words.
 template <int NP>
@@ -97,11 +31,6 @@ __device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log
     pack_words<NP, 4>(x, w);
 #pragma unroll
     for (int i = 0; i < 4; ++i) out[i] = w[i];
-}
-
-__device__ __forceinline__ void compose(u32& g, u32& p, u32 g_earlier, u32 p_earlier) {
-    g = g | (p & g_earlier);
-    p = p & p_earlier;
 }
 
 // Block-wide exclusive scan of carry (generate, propagate) pairs; returns the
@@ -138,17 +67,6 @@ __device__ __forceinline__ void block_scan_gp(u32& g, u32& p, u32& tg, u32& tp) 
     p = ep;
     tg = wg[nwarps - 1];
     tp = wp[nwarps - 1];
-}
-
-// Inclusive warp scan of (generate, propagate) pairs over the lanes.
-__device__ __forceinline__ void warp_scan_gp(u32& g, u32& p) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const u32 og = __shfl_up_sync(0xffffffffu, g, d);
-        const u32 op = __shfl_up_sync(0xffffffffu, p, d);
-        if (lane >= d) compose(g, p, og, op);
-    }
 }
 
 // Look-back state of a tile: bits 0-1 the state, bit 2 the generate bit (or, for
@@ -194,33 +112,12 @@ __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin)
 // (flags: [0] tile counter, [1] error word, [2 + t] state of tile t). Returns the
 // carry into the thread's first limb. Every thread of the CTA calls it (two
 // barriers).
-constexpr int kCrtPer = 4;
-static_assert(kCrtThreads * kCrtPer == kCrtTile, "four limbs per thread");
-
 __device__ __forceinline__ u32 tile_carry_in(const u32 (&gb)[kCrtPer], const u32 (&pb)[kCrtPer], u32 tile,
                                              u32* flags) {
-    constexpr int NW = kCrtThreads / 32;
-    __shared__ u32 s_wg[NW], s_wp[NW], s_cin;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    u32 G = gb[0], P = pb[0];
-#pragma unroll
-    for (int c = 1; c < kCrtPer; ++c) {
-        G = gb[c] | (pb[c] & G);
-        P = pb[c] & P;
-    }
-    u32 ig = G, ip = P;
-    warp_scan_gp(ig, ip);
-    u32 xg = __shfl_up_sync(0xffffffffu, ig, 1), xp = __shfl_up_sync(0xffffffffu, ip, 1);
-    if (lane == 0) { xg = 0; xp = 1; }
-    if (lane == 31) { s_wg[warp] = ig; s_wp[warp] = ip; }
-    __syncthreads();
+    __shared__ u32 s_cin;
+    u32 xg, xp, tg, tp;
+    tile_scan(gb, pb, xg, xp, tg, tp);
     if (threadIdx.x == 0) {
-        u32 tg = 0, tp = 1;  // the tile's (generate, propagate) pair
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-            tg = s_wg[w] | (s_wp[w] & tg);
-            tp = s_wp[w] & tp;
-        }
         u32* status = flags + 2;
         u32 cin = 0;
         if (tile > 0) {
@@ -235,30 +132,7 @@ __device__ __forceinline__ u32 tile_carry_in(const u32 (&gb)[kCrtPer], const u32
         s_cin = cin;
     }
     __syncthreads();
-    // the tile's carry-in through the earlier warps, then the earlier lanes
-    u32 c = s_cin;
-    for (int w = 0; w < warp; ++w) c = s_wg[w] | (s_wp[w] & c);
-    return xg | (xp & c);
-}
-
-// Adds the carries into a thread's four limbs and stores those below len.
-__device__ __forceinline__ void store_limbs(u64* __restrict__ dst, u64 k0, u64 len, const u64 (&sv)[kCrtPer],
-                                            const u32 (&gb)[kCrtPer], const u32 (&pb)[kCrtPer], u32 c) {
-    u64 out[kCrtPer];
-#pragma unroll
-    for (int i = 0; i < kCrtPer; ++i) {
-        out[i] = sv[i] + c;
-        c = gb[i] | (pb[i] & c);
-    }
-    u64* d = dst + k0;
-    if (k0 + kCrtPer <= len && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
-        reinterpret_cast<uint4*>(d)[0] = make_uint4((u32)out[0], (u32)(out[0] >> 32), (u32)out[1], (u32)(out[1] >> 32));
-        reinterpret_cast<uint4*>(d)[1] = make_uint4((u32)out[2], (u32)(out[2] >> 32), (u32)out[3], (u32)(out[3] >> 32));
-    } else {
-#pragma unroll
-        for (int i = 0; i < kCrtPer; ++i)
-            if (k0 + i < len) d[i] = out[i];
-    }
+    return xg | (xp & s_cin);
 }
 
 // Tile of kCrtTile output limbs, four per thread: thread t reconstructs the
@@ -272,20 +146,13 @@ __device__ __forceinline__ void store_limbs(u64* __restrict__ dst, u64 k0, u64 l
 // by the look-back.
 // flags: [0] tile counter, [1] error word, [2 + t] look-back state of tile t; all
 // zero when the kernel starts (the preceding transform kernel clears them).
-// u64 words of a reconstructed coefficient for NP primes below 2^31 (X < 2^(31 NP - 1)).
-__host__ __device__ constexpr int crt_limb_words(int np) {
-    return (31 * np - 1 + 63) / 64 < 4 ? (31 * np - 1 + 63) / 64 : 4;
-}
-
 template <int NP>
-__global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__ resid, int log_t,
+__global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restrict__ resid, int log_t,
                                                           u64 conv_len, u64 out_len, u64* __restrict__ dst,
                                                           u32* __restrict__ flags,
                                                           const __grid_constant__ CrtParams cp,
                                                           const ProductDesc* __restrict__ batch) {
     constexpr int L = crt_limb_words(NP);
-    constexpr int NW = kCrtThreads / 32;
-    constexpr int NE = L * (L - 1) / 2;  // words a thread takes from its predecessor
     if (batch) {  // member blockIdx.y of a batch: grid.x covers its largest member
         const ProductDesc& d = batch[blockIdx.y];
         resid = d.spec;
@@ -297,15 +164,13 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
     // Tiles are numbered in the order CTAs start, so a tile only ever waits for
     // tiles whose CTAs are already running.
     __shared__ u32 s_tile;
-    __shared__ u64 s_pre[L][L];              // the L coefficients before the tile
-    __shared__ u64 s_edge[NW][NE > 0 ? NE : 1];
-    __shared__ u32 s_edge_h[NW];
+    __shared__ u64 s_pre[L][L];  // the L coefficients before the tile
     if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
     __syncthreads();
     const u32 tile = s_tile;
     const u32 tiles = (u32)((out_len + kCrtTile - 1) / kCrtTile);
     if (tile >= tiles) return;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int t = threadIdx.x;
     const u64 j0 = (u64)tile * kCrtTile;
     const u64 k0 = j0 + (u64)t * kCrtPer;
     // Coefficients k0 .. k0 + 3 (zero past the convolution).
@@ -347,84 +212,9 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_mul(const u32* __restrict__
 #pragma unroll
         for (int i = 0; i < L; ++i) s_pre[t][i] = w[i];
     }
-    // Sum of limb c from words of coefficients c - w (own when c - w >= 0, else
-    // from prev[]): low word and overflow count.
-    auto limb = [&](int c, const u64 (&prev)[NE > 0 ? NE : 1], u32& h) -> u64 {
-        u64 lo = 0;
-        h = 0;
-#pragma unroll
-        for (int w = 0; w < L; ++w) {
-            u64 v;
-            if (c - w >= 0) {
-                v = cw[c - w][w];
-            } else {
-                // pair (w, c) with c < w: index w(w-1)/2 + c
-                v = prev[w * (w - 1) / 2 + c];
-            }
-            lo += v;
-            h += lo < v ? 1u : 0u;
-        }
-        return lo;
-    };
-    // What the successor needs: words w of coefficients 4 + c - w (c < w) and the
-    // overflow count of limb 3 (own words only).
-    u64 mine[NE > 0 ? NE : 1];
-#pragma unroll
-    for (int w = 1; w < L; ++w)
-#pragma unroll
-        for (int c = 0; c < w; ++c) mine[w * (w - 1) / 2 + c] = cw[kCrtPer + c - w][w];
-    u32 h3;
-    {
-        const u64 dummy[NE > 0 ? NE : 1] = {};
-        limb(kCrtPer - 1, dummy, h3);  // limb 3 uses own words only (L <= 4)
-    }
-    if (lane == 31) {
-#pragma unroll
-        for (int e = 0; e < NE; ++e) s_edge[warp][e] = mine[e];
-        s_edge_h[warp] = h3;
-    }
-    __syncthreads();
-    u64 prev[NE > 0 ? NE : 1];
-    u32 hprev;
-#pragma unroll
-    for (int e = 0; e < NE; ++e) prev[e] = __shfl_up_sync(0xffffffffu, mine[e], 1);
-    hprev = __shfl_up_sync(0xffffffffu, h3, 1);
-    if (lane == 0) {
-        if (warp > 0) {
-#pragma unroll
-            for (int e = 0; e < NE; ++e) prev[e] = s_edge[warp - 1][e];
-            hprev = s_edge_h[warp - 1];
-        } else {
-            // predecessor = the coefficients before the tile: coefficient j0 - L + i
-            // plays the predecessor's coefficient 4 - L + i
-#pragma unroll
-            for (int w = 1; w < L; ++w)
-#pragma unroll
-                for (int c = 0; c < w; ++c) prev[w * (w - 1) / 2 + c] = s_pre[L + c - w][w];
-            // overflow count of limb j0 - 1: words w of coefficients j0 - 1 - w
-            u64 lo = 0;
-            hprev = 0;
-#pragma unroll
-            for (int w = 0; w < L; ++w) {
-                const u64 v = s_pre[L - 1 - w][w];
-                lo += v;
-                hprev += lo < v ? 1u : 0u;
-            }
-        }
-    }
-    // Limb values before the carries, and their (generate, propagate) bits.
     u64 sv[kCrtPer];
     u32 gb[kCrtPer], pb[kCrtPer];
-#pragma unroll
-    for (int c = 0; c < kCrtPer; ++c) {
-        u32 h;
-        const u64 lo = limb(c, prev, h);
-        const u64 s2 = lo + hprev;
-        sv[c] = s2;
-        gb[c] = s2 < lo ? 1u : 0u;
-        pb[c] = s2 == ~0ull ? 1u : 0u;
-        hprev = h;
-    }
+    tile_limbs<L>(cw, s_pre, sv, gb, pb);
     store_limbs(dst, k0, out_len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags));
 }
 

@@ -77,6 +77,8 @@ struct TransformArgs {
     int op_count;      // operands of that pass; 0 means every operand of the member
     u32* flags;        // CRT look-back flags to clear (products), or null
     u32 flag_words;
+    u64* dst;          // product limbs of the fused one-kernel path (single member)
+    u64 out_len;
     PrimeSet ps;
 };
 
@@ -95,6 +97,12 @@ struct CrtParams {
 
 // Launchers; each returns the launch status.
 cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
+// Whole products of T <= 2^kFusedMaxLog points with kFusedPrimes primes in one
+// kernel: a cluster of one CTA per prime transforms, then reconstructs and carries
+// the product from the cluster's shared memory. Returns cudaErrorNotSupported for
+// other shapes (the caller then takes launch_small and the CRT kernel).
+constexpr int kFusedMaxLog = 12, kFusedPrimes = 5;
+cudaError_t launch_small_fused(const TransformArgs& g, const CrtParams& cp, bool square, cudaStream_t st);
 cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
 cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st);
 cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st);

@@ -18,6 +18,9 @@
 // compile-time constants.
 #include "launch.h"
 #include "ntt_passes.cuh"
+#include "crt.cuh"
+
+#include <cooperative_groups.h>
 
 #include <algorithm>
 
@@ -117,6 +120,100 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     dit_full<A, LOG_N, kThreads, 1, VS>(sa, pp.inv, pp.p);
     u32* out = m.spec + ((size_t)blockIdx.x << LOG_N);
     for (int i = threadIdx.x; i < (int)m.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
+}
+
+// A whole product of T = 2^LOG_N <= 2^12 points in one kernel: a cluster of NP
+// CTAs, one per prime, runs the one-CTA transform of k_small and keeps its
+// canonical residues in shared memory; after a cluster barrier CTA r reconstructs
+// output tile r (kCrtTile limbs, four per thread) from every CTA's residues
+// through distributed shared memory, publishes the tile's (generate, propagate)
+// pair, and after a second barrier takes the carry of the earlier tiles from their
+// pairs. No residue leaves the chip and the product costs one launch.
+// grid = (NP, members), cluster = (NP, 1, 1).
+template <bool SQUARE, int LOG_N, int NP>
+__global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant__ TransformArgs g,
+                                                          const __grid_constant__ CrtParams cp) {
+    using A = LazyArith;
+    namespace cg = cooperative_groups;
+    extern __shared__ u32 sm[];
+    constexpr int N = 1 << LOG_N;
+    constexpr int VS = padded_len(N);
+    constexpr int L = crt_limb_words(NP);
+    static_assert(kThreads == kCrtThreads, "one CRT tile per CTA of the transform's size");
+    cg::cluster_group cluster = cg::this_cluster();
+    const int prime = (int)cluster.block_rank();
+    const PrimeParams& pp = g.ps.pr[prime];
+    const Member m = member_of(g, blockIdx.y, SQUARE);
+    u64* dst = g.dst;
+    u64 out_len = g.out_len;
+    if (g.batch) {
+        dst = g.batch[blockIdx.y].dst;
+        out_len = g.batch[blockIdx.y].out_len;
+    }
+    u32* sa = sm;
+    u32* sb = sm + VS;
+    for (int i = threadIdx.x; i < N; i += kThreads) {
+        sa[pad_index(i)] = (u64)i < m.la ? reduce_coefficient<A, false>(__ldg(m.a + i), pp) : 0u;
+        if (!SQUARE) sb[pad_index(i)] = (u64)i < m.lb ? reduce_coefficient<A, false>(__ldg(m.b + i), pp) : 0u;
+    }
+    __syncthreads();
+    dif_full<A, LOG_N, kThreads, SQUARE ? 1 : 2, VS>(sm, pp.fwd, pp.p);
+    for (int i = threadIdx.x; i < N; i += kThreads) {
+        const int k = pad_index(i);
+        const u32 x = sa[k];
+        const u32 y = SQUARE ? x : sb[k];
+        sa[k] = A::mulc(A::pointwise(x, y, pp.p, pp.pni), pp.scale, pp.p);
+    }
+    __syncthreads();
+    dit_full<A, LOG_N, kThreads, 1, VS>(sa, pp.inv, pp.p);
+    for (int i = threadIdx.x; i < N; i += kThreads) sa[pad_index(i)] = A::canonical(sa[pad_index(i)], pp.p);
+    cluster.sync();  // every prime's residues are in place
+    __shared__ u64 s_pre[L][L];
+    __shared__ u32 s_pair;
+    const u64 conv_len = m.conv_len;
+    const u32 tiles = (u32)((out_len + kCrtTile - 1) / kCrtTile);
+    const bool active = (u32)prime < tiles;
+    const int t = threadIdx.x;
+    const u64 j0 = (u64)prime * kCrtTile, k0 = j0 + (u64)t * kCrtPer;
+    const u32* res[NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) res[i] = cluster.map_shared_rank(sa, i);
+    auto coefficient = [&](u64 k, u64 (&w)[L]) {
+        u32 r[NP], x[NP + 1];
+#pragma unroll
+        for (int i = 0; i < NP; ++i) r[i] = k < conv_len ? res[i][pad_index((int)k)] : 0u;
+        crt_words<NP>(r, cp, x);
+        pack_words<NP, L>(x, w);
+    };
+    u64 sv[kCrtPer];
+    u32 gb[kCrtPer], pb[kCrtPer], xg = 0, xp = 1;
+    if (active) {  // the same branch for the whole CTA
+        u64 cw[kCrtPer][L];
+#pragma unroll
+        for (int c = 0; c < kCrtPer; ++c) coefficient(k0 + c, cw[c]);
+        if (t < L) {  // coefficient j0 - L + t, before the tile
+            u64 w[L];
+#pragma unroll
+            for (int i = 0; i < L; ++i) w[i] = 0;
+            if (j0 >= (u64)(L - t)) coefficient(j0 - (u64)(L - t), w);
+#pragma unroll
+            for (int i = 0; i < L; ++i) s_pre[t][i] = w[i];
+        }
+        tile_limbs<L>(cw, s_pre, sv, gb, pb);
+        u32 tg, tp;
+        tile_scan(gb, pb, xg, xp, tg, tp);
+        if (t == 0) s_pair = tg | (tp << 1);
+    }
+    cluster.sync();  // every tile's pair is published
+    if (active) {
+        u32 cin = 0;  // carry out of tiles 0 .. prime-1
+        for (int j = 0; j < prime; ++j) {
+            const u32 a = *cluster.map_shared_rank(&s_pair, j);
+            cin = (a & 1u) | ((a >> 1) & cin);
+        }
+        store_limbs(dst, k0, out_len, sv, gb, pb, xg | (xp & cin));
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // Copies the level-major root table of a 2^LOG_N-point transform (entries below
@@ -689,6 +786,40 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
     return cudaGetLastError();
 }
 
+template <int L>
+static cudaError_t fused_at(const TransformArgs& g, const CrtParams* cp, bool square, cudaStream_t st, bool init) {
+    auto k = square ? k_small_fused<true, L, kFusedPrimes> : k_small_fused<false, L, kFusedPrimes>;
+    if (init) return opt_in(k);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kFusedPrimes, g.batch ? g.count : 1);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kFusedPrimes;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, g, *cp);
+}
+
+static cudaError_t fused_any(const TransformArgs& g, const CrtParams* cp, bool square, cudaStream_t st, bool init) {
+    switch (g.log_t) {
+        case 4: return fused_at<4>(g, cp, square, st, init);
+        case 5: return fused_at<5>(g, cp, square, st, init);
+        case 6: return fused_at<6>(g, cp, square, st, init);
+        case 7: return fused_at<7>(g, cp, square, st, init);
+        case 8: return fused_at<8>(g, cp, square, st, init);
+        case 9: return fused_at<9>(g, cp, square, st, init);
+        case 10: return fused_at<10>(g, cp, square, st, init);
+        case 11: return fused_at<11>(g, cp, square, st, init);
+        case 12: return fused_at<12>(g, cp, square, st, init);
+        default: return cudaErrorNotSupported;
+    }
+}
+
 static cudaError_t small_any(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     switch (g.log_t) {
         case 4: return small_at<LazyArith, 4>(g, square, sign, st, init);
@@ -752,6 +883,12 @@ static cudaError_t inv_cols_any(const TransformArgs& g, cudaStream_t st, bool in
     }
 }
 
+cudaError_t launch_small_fused(const TransformArgs& g, const CrtParams& cp, bool square, cudaStream_t st) {
+    if (g.wide || g.np != kFusedPrimes || cp.np != kFusedPrimes || g.log_t > kFusedMaxLog || g.log_t < 4)
+        return cudaErrorNotSupported;
+    return fused_any(g, &cp, square, st, false);
+}
+
 cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
     return small_any(g, square, sign, st, false);
 }
@@ -773,6 +910,7 @@ cudaError_t init_transform_kernels() {
             for (int l = 4; l <= 13 && e == cudaSuccess; ++l) {
                 g.log_t = l;
                 e = small_any(g, sq, sg, 0, true);
+                if (e == cudaSuccess && !sg && l <= kFusedMaxLog) e = fused_any(g, nullptr, sq, 0, true);
             }
             for (int w = 0; w < 2; ++w) {
                 g.wide = w;
