@@ -244,6 +244,30 @@ def configs_section(dev, stream, peak_gbs: float) -> list:
                     "algorithmic_bytes": model, "roofline_frac": round(model / (ms / 1000.0) / 1e9 / peak_gbs, 4)})
         del a, b, d
     ws.close()
+    # Convolutions of 16-bit coefficients (the reference's published conv sizes,
+    # README.md:33-36 of the reference), operands resident.
+    cws = ntt.GpuConvWorkspace()
+    for n, reps in ((1024, 4000), (65536, 1000), (1 << 20, 100), (1 << 22, 20)):
+        plan = ntt.ConvPlan.new(n, n, 0xFFFF, 0xFFFF, False)
+        assert cws.prepare(plan), ntt.last_error()
+        a = torch.from_numpy((operand(n, 1) & np.uint64(0xFFFF)).view(np.int64)).to(dev)
+        b = torch.from_numpy((operand(n, 2) & np.uint64(0xFFFF)).view(np.int64)).to(dev)
+        d = torch.empty(plan.output_len(), dtype=torch.int64, device=dev)
+        for _ in range(3):
+            assert cws.convolve_device(d, a, b, stream), ntt.last_error()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            cws.convolve_device(d, a, b, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        out.append({"config": f"conv 16-bit {n}", "ms_per_product": round(ms, 5),
+                    "products_per_s": round(1000.0 / ms, 1), "primes": plan.primes,
+                    "log_transform": plan.log_transform})
+        del a, b, d
+    cws.close()
     torch.cuda.empty_cache()
     return out
 

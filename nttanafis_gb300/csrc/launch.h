@@ -101,7 +101,7 @@ cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStr
 // kernel: a cluster of one CTA per prime transforms, then reconstructs and carries
 // the product from the cluster's shared memory. Returns cudaErrorNotSupported for
 // other shapes (the caller then takes launch_small and the CRT kernel).
-constexpr int kFusedMaxLog = 12, kFusedPrimes = 5;
+constexpr int kFusedMaxLog = 13, kFusedPrimes = 5;
 cudaError_t launch_small_fused(const TransformArgs& g, const CrtParams& cp, bool square, cudaStream_t st);
 cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
 cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st);

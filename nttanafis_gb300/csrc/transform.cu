@@ -122,10 +122,10 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     for (int i = threadIdx.x; i < (int)m.conv_len; i += kThreads) out[i] = A::canonical(sa[pad_index(i)], pp.p);
 }
 
-// A whole product of T = 2^LOG_N <= 2^12 points in one kernel: a cluster of NP
+// A whole product of T = 2^LOG_N <= 2^13 points in one kernel: a cluster of NP
 // CTAs, one per prime, runs the one-CTA transform of k_small and keeps its
 // canonical residues in shared memory; after a cluster barrier CTA r reconstructs
-// output tile r (kCrtTile limbs, four per thread) from every CTA's residues
+// output tiles r, r + NP, ... (kCrtTile limbs, four per thread) from every CTA's residues
 // through distributed shared memory, publishes the tile's (generate, propagate)
 // pair, and after a second barrier takes the carry of the earlier tiles from their
 // pairs. No residue leaves the chip and the product costs one launch.
@@ -168,13 +168,13 @@ __global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant_
     dit_full<A, LOG_N, kThreads, 1, VS>(sa, pp.inv, pp.p);
     for (int i = threadIdx.x; i < N; i += kThreads) sa[pad_index(i)] = A::canonical(sa[pad_index(i)], pp.p);
     cluster.sync();  // every prime's residues are in place
+    // CTA r reconstructs output tiles r, r + NP, ... (at most MT of them).
+    constexpr int MT = ((N + kCrtTile) / kCrtTile + NP - 1) / NP;
     __shared__ u64 s_pre[L][L];
-    __shared__ u32 s_pair;
+    __shared__ u32 s_pair[MT];
     const u64 conv_len = m.conv_len;
     const u32 tiles = (u32)((out_len + kCrtTile - 1) / kCrtTile);
-    const bool active = (u32)prime < tiles;
     const int t = threadIdx.x;
-    const u64 j0 = (u64)prime * kCrtTile, k0 = j0 + (u64)t * kCrtPer;
     const u32* res[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) res[i] = cluster.map_shared_rank(sa, i);
@@ -185,9 +185,13 @@ __global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant_
         crt_words<NP>(r, cp, x);
         pack_words<NP, L>(x, w);
     };
-    u64 sv[kCrtPer];
-    u32 gb[kCrtPer], pb[kCrtPer], xg = 0, xp = 1;
-    if (active) {  // the same branch for the whole CTA
+    u64 sv[MT][kCrtPer];
+    u32 gb[MT][kCrtPer], pb[MT][kCrtPer], xg[MT], xp[MT];
+#pragma unroll
+    for (int q = 0; q < MT; ++q) {
+        const u32 tile = (u32)prime + (u32)q * NP;
+        if (tile >= tiles) break;  // the same for the whole CTA
+        const u64 j0 = (u64)tile * kCrtTile, k0 = j0 + (u64)t * kCrtPer;
         u64 cw[kCrtPer][L];
 #pragma unroll
         for (int c = 0; c < kCrtPer; ++c) coefficient(k0 + c, cw[c]);
@@ -199,19 +203,22 @@ __global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant_
 #pragma unroll
             for (int i = 0; i < L; ++i) s_pre[t][i] = w[i];
         }
-        tile_limbs<L>(cw, s_pre, sv, gb, pb);
+        tile_limbs<L>(cw, s_pre, sv[q], gb[q], pb[q]);
         u32 tg, tp;
-        tile_scan(gb, pb, xg, xp, tg, tp);
-        if (t == 0) s_pair = tg | (tp << 1);
+        tile_scan(gb[q], pb[q], xg[q], xp[q], tg, tp);
+        if (t == 0) s_pair[q] = tg | (tp << 1);
     }
     cluster.sync();  // every tile's pair is published
-    if (active) {
-        u32 cin = 0;  // carry out of tiles 0 .. prime-1
-        for (int j = 0; j < prime; ++j) {
-            const u32 a = *cluster.map_shared_rank(&s_pair, j);
+#pragma unroll
+    for (int q = 0; q < MT; ++q) {
+        const u32 tile = (u32)prime + (u32)q * NP;
+        if (tile >= tiles) break;
+        u32 cin = 0;  // carry out of tiles 0 .. tile-1 (tile j sits in CTA j mod NP)
+        for (u32 j = 0; j < tile; ++j) {
+            const u32 a = *cluster.map_shared_rank(&s_pair[j / NP], (int)(j % NP));
             cin = (a & 1u) | ((a >> 1) & cin);
         }
-        store_limbs(dst, k0, out_len, sv, gb, pb, xg | (xp & cin));
+        store_limbs(dst, (u64)tile * kCrtTile + (u64)t * kCrtPer, out_len, sv[q], gb[q], pb[q], xg[q] | (xp[q] & cin));
     }
     cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
@@ -816,6 +823,7 @@ static cudaError_t fused_any(const TransformArgs& g, const CrtParams* cp, bool s
         case 10: return fused_at<10>(g, cp, square, st, init);
         case 11: return fused_at<11>(g, cp, square, st, init);
         case 12: return fused_at<12>(g, cp, square, st, init);
+        case 13: return fused_at<13>(g, cp, square, st, init);
         default: return cudaErrorNotSupported;
     }
 }
