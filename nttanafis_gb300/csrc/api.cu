@@ -632,12 +632,6 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
     } else {
         ta.log_r = g.log_t / 2;
         ta.log_c = g.log_t - ta.log_r;
-        const int G = std::min(32, std::max(8, (1 << kMaxBlockLog) >> ta.log_r));
-        ta.log_g = __builtin_ctz(G);
-        int vs = ta.log_r >= 5 ? (1 << ta.log_r) + (1 << (ta.log_r - 5)) : (1 << ta.log_r);
-        const int target = 32 / G;
-        vs += ((target - vs) % 32 + 32) % 32;
-        ta.vstride_col = vs;
         if (b_ready && !square) {
             g_launches += 1;
             ta.op_count = 1;

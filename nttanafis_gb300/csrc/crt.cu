@@ -10,10 +10,12 @@
 // Here every product coefficient is a 64-bit-limb convolution value, so coefficient
 // k lands at limb k and spans l64 limbs. One CTA owns 1024 output limbs: it
 // reconstructs the coefficients that reach them, sums the overlapping windows,
-// propagates carries inside the tile with a generate/propagate block scan and
+// propagates carries inside the tile with a generate/propagate scan (crt.cuh) and
 // resolves the tile's carry-in with a decoupled look-back over the earlier tiles'
 // published (generate, propagate) pairs, so the limbs are written once, final.
 // Every look-back wait is bounded; a wait that gives up is counted and flagged.
+// The same file holds the big-integer addition of the block split (k_add_limbs)
+// and the descriptors of its blocks (k_split_descs).
 #include "crt.cuh"
 #include "launch.h"
 
@@ -31,42 +33,6 @@ __device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log
     pack_words<NP, 4>(x, w);
 #pragma unroll
     for (int i = 0; i < 4; ++i) out[i] = w[i];
-}
-
-// Block-wide exclusive scan of carry (generate, propagate) pairs; returns the
-// exclusive pair in (g, p) and the inclusive total of the block in (tg, tp).
-__device__ __forceinline__ void block_scan_gp(u32& g, u32& p, u32& tg, u32& tp) {
-    __shared__ u32 wg[32], wp[32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nwarps = (blockDim.x + 31) >> 5;
-    u32 ig = g, ip = p;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const u32 og = __shfl_up_sync(0xffffffffu, ig, d);
-        const u32 op = __shfl_up_sync(0xffffffffu, ip, d);
-        if (lane >= d) compose(ig, ip, og, op);
-    }
-    if (lane == 31) { wg[warp] = ig; wp[warp] = ip; }
-    __syncthreads();
-    if (warp == 0) {
-        u32 a = lane < nwarps ? wg[lane] : 0u, b = lane < nwarps ? wp[lane] : 1u;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const u32 og = __shfl_up_sync(0xffffffffu, a, d);
-            const u32 op = __shfl_up_sync(0xffffffffu, b, d);
-            if (lane >= d) compose(a, b, og, op);
-        }
-        if (lane < nwarps) { wg[lane] = a; wp[lane] = b; }
-    }
-    __syncthreads();
-    // exclusive inside the warp
-    u32 eg = __shfl_up_sync(0xffffffffu, ig, 1), ep = __shfl_up_sync(0xffffffffu, ip, 1);
-    if (lane == 0) { eg = 0; ep = 1; }
-    if (warp > 0) compose(eg, ep, wg[warp - 1], wp[warp - 1]);
-    g = eg;
-    p = ep;
-    tg = wg[nwarps - 1];
-    tp = wp[nwarps - 1];
 }
 
 // Look-back state of a tile: bits 0-1 the state, bit 2 the generate bit (or, for

@@ -70,8 +70,6 @@ struct TransformArgs {
     int np;            // primes
     int log_t;         // log2 transform length
     int log_r, log_c;  // four-step split T = R * C (unused on the one-CTA path)
-    int log_g;         // log2 columns per CTA in the column passes
-    int vstride_col;   // padded words per column vector in shared memory
     int wide;          // 1: primes up to 2^31 in canonical arithmetic; 0: lazy, p < 2^30
     int op_base;       // first operand of a single-member column pass (0: a, 1: b)
     int op_count;      // operands of that pass; 0 means every operand of the member

@@ -7,13 +7,17 @@
 // inverse leaves for long rows, src/multiply/schedule.rs:259-279), inverse with the
 // N^-1 scale (src/transform/inverse.rs:52-218, src/multiply/schedule.rs:225-252).
 //
-// Two layouts:
-//  * one CTA per prime holds the whole transform (T <= 2^13): k_small;
-//  * four-step for T = R*C > 2^13: k_fwd_cols (pack + column DIF + twiddle),
-//    k_rows (row DIF of a and b, pointwise, row DIT, inverse twiddle) and
-//    k_inv_cols (column DIT + canonical residues). The spectrum order between the
-//    passes is the four-step's transposed, bit-reversed order; only the inverse
-//    reads it, so no transpose is ever materialised.
+// Layouts:
+//  * one CTA per prime holds the whole transform (T <= 2^13): k_small, and for
+//    products k_small_fused, a cluster of one CTA per prime that also
+//    reconstructs and carries the product through distributed shared memory;
+//  * four-step for T = R*C > 2^13: k_fwd_cols (pack + column DIF + twiddle; for
+//    R = 2^10 k_fwd_cols2, two radix-32 passes), k_rows (row DIF of a and b,
+//    pointwise, row DIT, inverse twiddle) and k_inv_cols (column DIT + canonical
+//    residues; for R = 2^10 k_inv_cols2). The spectrum order between the passes is
+//    the four-step's transposed, bit-reversed order; only the inverse reads it, so
+//    no transpose is ever materialised.
+//  * k_step_tables builds the four-step factor tables of a transform length.
 // Every kernel is instantiated per transform size so all shared-memory strides are
 // compile-time constants.
 #include "launch.h"
