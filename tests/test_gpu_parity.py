@@ -290,3 +290,40 @@ def test_concurrent_host_calls_and_streams(gpu):
         assert np.array_equal(out.cpu().numpy().view(np.uint64), expected[(la, lb)]), (la, lb)
     for w in wss:
         w.close()
+
+
+def test_six_prime_products(ws, gpu):
+    # T = 2^22 and 2^23 with the shorter operand above 2^20 limbs need six primes
+    for la, lb in [(1 << 21, 1 << 21), (3 << 20, (1 << 21) + 3)]:
+        assert gpu.MulPlan.new(la, lb).primes == 6
+        a, b = operand(la, 111), operand(lb, 112)
+        assert fingerprint_ok(a, b, gpu_mul(ws, a, b)), (la, lb)
+    ones = np.full(1 << 21, MASK, dtype=np.uint64)
+    assert np.array_equal(gpu_mul(ws, ones, ones), all_ones_expected(1 << 21, 1 << 21))
+
+
+def test_poisoned_scratch_and_any_shape_order(gpu):
+    # caller scratch full of ones (no kernel may rely on its contents), and one
+    # workspace serving fused, four-step and split shapes in a shuffled order
+    import torch
+
+    shapes = [(3000, 2000), (70000, 50000), (90000, 2000), (1024, 1024), (5, 7), (1 << 17, 1 << 17), (40000, 300)]
+    expected = {s: oracle.mul(operand(s[0], 121), operand(s[1], 122), THREADS) for s in shapes}
+    stream = torch.cuda.current_stream()
+    for la, lb in shapes:
+        plan = gpu.MulPlan.new(la, lb)
+        da = torch.from_numpy(operand(la, 121).view(np.int64)).cuda()
+        db = torch.from_numpy(operand(lb, 122).view(np.int64)).cuda()
+        scratch = torch.full((max(1, plan.scratch_len()),), -1, dtype=torch.int64, device="cuda")
+        dst = torch.full((la + lb,), -1, dtype=torch.int64, device="cuda")
+        assert plan.mul_device(dst, da, db, scratch, stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(dst.cpu().numpy().view(np.uint64), expected[(la, lb)]), (la, lb)
+    w = gpu.GpuMulWorkspace()
+    rng = np.random.default_rng(5)
+    for i in rng.permutation(len(shapes * 3)):
+        la, lb = (shapes * 3)[i]
+        dst = np.full(la + lb, MASK, dtype=np.uint64)
+        assert w.mul(dst, operand(la, 121), operand(lb, 122))
+        assert np.array_equal(dst, expected[(la, lb)]), (la, lb)
+    w.close()
