@@ -19,6 +19,9 @@ Printed keys beyond the base contract:
   roofline    algorithmic bytes of one product (operands in, product out, and the
               fused four-step spectrum traffic 8*S with S from the reference
               planner) over the measured device time per product;
+  compute_roofline  the transforms' butterflies per product over the device time,
+              against the butterfly rate of a register-only probe (no memory
+              traffic) run on the same GPU: the integer-issue ceiling;
   kernels     per-kernel device times from CUDA events recorded between the
               library's launches on the launching stream;
   cpu_baseline  the oracle (a C restatement of the reference algorithm) timed
@@ -602,6 +605,13 @@ def run_gpu(args) -> None:
         except Exception:
             traffic = None
 
+    # Compute ceiling: the transforms' butterflies against a register-only probe of
+    # the same lazy butterfly (no memory traffic) measured now on this GPU.
+    t_len = 1 << plan.log_transform
+    butterflies = 3 * plan.primes * (t_len // 2) * plan.log_transform
+    probe_rate = ntt.butterfly_rate()
+    bfly_rate = butterflies / (ms_per_step / 1000.0)
+
     line = {
         "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -619,6 +629,11 @@ def run_gpu(args) -> None:
                      "traffic": traffic, "algorithmic_bytes": model,
                      "unit_of_launch": "one product (the fused kernel sequence below)",
                      "dominant_kernel": kernel_names[dominant] if dominant is not None else None},
+        "compute_roofline": {"bound": "integer issue", "achieved": bfly_rate, "peak": probe_rate,
+                             "unit": "butterflies/s", "frac": bfly_rate / probe_rate,
+                             "butterflies_per_product": butterflies,
+                             "floor_ms": butterflies / probe_rate * 1000.0,
+                             "peak_kind": "measured now: register-only lazy-butterfly probe (ntt_probe_butterflies)"},
         "kernels": kernels, "kernels_ms_total": instrumented_ms,
         "gpu_launches": launches, "wall_s": t_wall,
         "parity": {"fingerprint_ok": fingerprint_ok, "lookback_timeouts": ntt.lookback_timeouts()},

@@ -203,6 +203,13 @@ uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const uint64_t* 
 int ntt_timing_start(int count);
 int ntt_timing_stop(float* ms, int capacity);
 
+/* Compute ceiling of the transforms, for measurement tools: runs `blocks` CTAs of
+ * 256 threads, each thread doing `iters` register-only radix-16 passes (32 lazy
+ * butterflies per pass) with no memory traffic, and writes the milliseconds of the
+ * timed launch (after one shorter warm-up launch) to *ms. Synchronizes the device.
+ * No reference counterpart. */
+uint8_t ntt_probe_butterflies(int blocks, int iters, float* ms);
+
 /* ---------------------------------------------------------------------------
  * Batched modular arithmetic in 50-bit prime fields (the reference's PrimeField
  * and CrtPair, src/field/prime_field.rs), on device arrays of residues (uint64_t,

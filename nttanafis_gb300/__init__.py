@@ -9,6 +9,7 @@ from .api import (  # noqa: F401
     GpuMulWorkspace,
     Request,
     MulPlan,
+    butterfly_rate,
     exported_symbols,
     kernel_launches,
     last_error,

@@ -102,6 +102,7 @@ _SIGNATURES = [
     ("ntt_timing_start", ctypes.c_int, [ctypes.c_int]),
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_lookback_timeouts", ctypes.c_uint32, []),
+    ("ntt_probe_butterflies", ctypes.c_uint8, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("ntt_field_check", ctypes.c_int, [ctypes.c_uint64]),
     ("ntt_field_mul_method", ctypes.c_int, [ctypes.c_int]),
     ("ntt_field_below", ctypes.c_uint64, [ctypes.c_uint64]),
@@ -162,6 +163,15 @@ def kernel_launches() -> int:
 def lookback_timeouts() -> int:
     """Bounded look-back waits of the CRT carry scan that gave up (expected 0)."""
     return int(library().ntt_lookback_timeouts())
+
+
+def butterfly_rate(blocks: int = 152 * 8, iters: int = 2000) -> float:
+    """Lazy butterflies per second of a register-only probe (no memory traffic):
+    the integer-issue ceiling of the transform kernels on this GPU."""
+    ms = ctypes.c_float(0.0)
+    if not library().ntt_probe_butterflies(blocks, iters, ctypes.byref(ms)):
+        raise RuntimeError(last_error())
+    return blocks * 256 * iters * 32 / (ms.value * 1e-3)
 
 
 def _host(arr: np.ndarray, name: str) -> np.ndarray:
