@@ -159,6 +159,7 @@ u32 lookback_timeouts();
 void set_last_error(const std::string& message);
 
 // One-time kernel attribute setup (shared-memory opt-in) for the current device.
+cudaError_t init_small_kernels();      // small.cu (called by init_transform_kernels)
 cudaError_t init_transform_kernels();
 cudaError_t init_crt_kernels();
 

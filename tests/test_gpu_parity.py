@@ -97,6 +97,21 @@ def test_unbalanced_either_order(ws):
         assert np.array_equal(gpu_mul(ws, short, long), oracle.mul(short, long))
 
 
+@pytest.mark.parametrize("log_t", range(4, 14))
+def test_fused_cluster_every_size(ws, log_t):
+    # every single-product fused size (T = 2^4 .. 2^13): products that fill T,
+    # squares, and all-ones operands whose carries run across every CRT tile
+    half = 1 << (log_t - 1)
+    a, b = operand(half, 31 + log_t), operand(half, 61 + log_t)
+    assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b)), log_t
+    assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a)), log_t
+    ones = np.full(half, MASK, dtype=np.uint64)
+    assert np.array_equal(gpu_mul(ws, ones, ones), all_ones_expected(half, half)), log_t
+    assert np.array_equal(gpu_sqr(ws, ones), all_ones_expected(half, half)), log_t
+    c = operand(half - 3, 91 + log_t)
+    assert np.array_equal(gpu_mul(ws, a, c), oracle.mul(a, c)), log_t
+
+
 @pytest.mark.parametrize("la,lb", [(4096, 4096), (4097, 4096), (8192, 8191), (8193, 8192), (20000, 13000),
                                    (65536, 65536), (65536, 256), (131072, 131072), (300000, 250000),
                                    (1 << 20, 131072)])
