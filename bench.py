@@ -298,10 +298,16 @@ def batched_section(dev, stream, count: int = 4096, reps: int = 3) -> dict:
         singles.append((d, a, b))
         limbs += s.la + s.lb
     batch = ntt.GpuBatch()
+    direct = ntt.GpuBatch()  # one stream, no graph: the layer without its scheduler
+    direct.set_graphs(False)
+    direct.set_lanes(1)
     packed = ntt.GpuBatch.pack(reqs)
     ws = ntt.GpuMulWorkspace()
-    # warm-up (tables, arenas) of both forms
-    assert batch.run(packed, stream), ntt.last_error()
+    # warm-up (tables, arenas) of every form; the batch tunes its lane count on runs
+    # 2-7 of this composition and captures the winner into a graph at run 8
+    for _ in range(8):
+        assert batch.run(packed, stream), ntt.last_error()
+    assert direct.run(packed, stream), ntt.last_error()
     for d, a, b in singles[:64]:
         assert ws.mul_device(d, a, b, stream), ntt.last_error()
     torch.cuda.synchronize(dev)
@@ -319,9 +325,26 @@ def batched_section(dev, stream, count: int = 4096, reps: int = 3) -> dict:
             best = min(best, max(e0.elapsed_time(e1) / 1000.0, time.perf_counter() - t0))
         return best
 
+    def steady(b, runs: int = 10) -> float:
+        # back-to-back runs on one stream: the host plans run i+1 while run i executes
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(runs):
+            b.run(packed, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return max(e0.elapsed_time(e1) / 1000.0, time.perf_counter() - t0) / runs
+
     launches0 = ntt.kernel_launches()
+    replays0 = batch.graph_replays
     t_batch = timed(lambda: batch.run(packed, stream))
     batch_launches = (ntt.kernel_launches() - launches0) // reps
+    graph_replays = batch.graph_replays - replays0
+    t_direct = timed(lambda: direct.run(packed, stream))
+    t_steady, t_steady_direct = steady(batch), steady(direct)
+    stats = batch.stats()
     # parity of a sample of members against single calls
     sample_ok = True
     import random
@@ -338,14 +361,20 @@ def batched_section(dev, stream, count: int = 4096, reps: int = 3) -> dict:
     t_plain = timed(lambda: [ws.mul_device(d, a, b, stream) for d, a, b in singles])
     plain_launches = (ntt.kernel_launches() - launches0) // reps
     batch.close()
+    direct.close()
     ws.close()
     return {
         "workload": f"{count} products, log-uniform 256..65536 limbs, ratio <= 8:1, 25% squares (seed 5)",
         "products_per_s": count / t_batch, "plain_products_per_s": count / t_plain,
-        "speedup_vs_plain": t_plain / t_batch, "ms_batch": 1000 * t_batch, "ms_plain": 1000 * t_plain,
+        "graph_replays": graph_replays, "tuned_lanes": stats["last_lanes"],
+        "steady_products_per_s": count / t_steady,
+        "one_stream_no_graph": {"products_per_s": count / t_direct, "steady_products_per_s": count / t_steady_direct},
+        "speedup_vs_plain": t_plain / t_batch, "steady_speedup_vs_plain": t_plain / t_steady,
+        "ms_batch": 1000 * t_batch, "ms_plain": 1000 * t_plain,
         "launches_batch": batch_launches, "launches_plain": plain_launches, "limbs_in": limbs,
         "parity_sample_ok": sample_ok,
-        "timing": "best of 3, max(device events, host wall) per enqueue+completion",
+        "timing": ("products_per_s: best of 3 single runs, max(device events, host wall) per enqueue+completion; "
+                   "steady_products_per_s: 10 back-to-back runs"),
     }
 
 

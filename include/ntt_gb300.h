@@ -167,10 +167,27 @@ typedef struct ntt_batch ntt_batch;
 ntt_batch* ntt_batch_new(void);
 void ntt_batch_free(ntt_batch* batch);
 /* Enqueues every request on `stream`: members are grouped by transform class and
- * each class runs as one launch per kernel. Returns 0 and launches nothing when a
- * request has no plan or a short dst (message in ntt_last_error()). */
+ * each class runs as one launch per kernel; the classes run concurrently on 1, 2
+ * or 4 streams of the batch (forked from and joined back into `stream`). A
+ * composition (the sequence of classes with their member counts and longest
+ * results) seen once runs with a lane count picked from its size; one that
+ * repeats is tuned on its own runs (runs 2 to 7 time each lane count twice with
+ * CUDA events on `stream`), then captured with the fastest lane count into a CUDA
+ * graph that serves every later run (not on the legacy default stream). Returns 0
+ * and launches nothing when a request has no plan or a short dst, or while
+ * `stream` is being captured by the caller (message in ntt_last_error()). */
 uint8_t ntt_batch_run_device(ntt_batch* batch, const ntt_request* requests, size_t count,
                              void* stream);
+/* Graph replay on (1) or off (0) for this batch (default on); other values only
+ * report. Returns the previous setting, -1 for a null batch. */
+int ntt_batch_set_graphs(ntt_batch* batch, int on);
+/* Lane count of every run: 1, 2 or 4 fixes it (no tuning), 0 returns to tuning
+ * per composition (the default); other values only report. Returns the previous
+ * setting, -1 for a null batch. */
+int ntt_batch_set_lanes(ntt_batch* batch, int lanes);
+/* out[0] runs served from a captured graph, out[1] compositions tuned, out[2]
+ * lanes of the last run enqueued directly or captured, out[3] compositions held. */
+void ntt_batch_stats(const ntt_batch* batch, uint64_t* out);
 
 /* Largest product (a_len + b_len - 1 coefficients) of ntt_mul_noalloc_device, and
  * the device memory its static arrays hold on every GPU that loads the library. */

@@ -96,6 +96,9 @@ _SIGNATURES = [
     ("ntt_batch_new", ctypes.c_void_p, []),
     ("ntt_batch_free", None, [ctypes.c_void_p]),
     ("ntt_batch_run_device", ctypes.c_uint8, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_batch_set_graphs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("ntt_batch_set_lanes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("ntt_batch_stats", None, [ctypes.c_void_p, ctypes.c_void_p]),
     ("ntt_mul_noalloc_device", ctypes.c_uint8,
      [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p]),
@@ -445,3 +448,25 @@ class GpuBatch:
         arr = requests if isinstance(requests, ctypes.Array) else self.pack(requests)
         return bool(self._lib.ntt_batch_run_device(self._b, ctypes.cast(arr, ctypes.c_void_p), len(arr),
                                                    _stream_handle(stream)))
+
+    def set_graphs(self, on: bool) -> bool:
+        """Turns CUDA-graph replay of repeated batch compositions on or off; returns
+        the previous setting."""
+        return bool(self._lib.ntt_batch_set_graphs(self._b, 1 if on else 0))
+
+    def set_lanes(self, lanes: int) -> int:
+        """Fixes the streams (1, 2 or 4) the classes of a run spread over, or with 0
+        lets the batch tune them per composition; returns the previous setting."""
+        return int(self._lib.ntt_batch_set_lanes(self._b, int(lanes)))
+
+    def stats(self) -> dict:
+        """Graph replays, compositions tuned, lanes of the last enqueued run and
+        compositions held by this batch object."""
+        out = (ctypes.c_uint64 * 4)()
+        self._lib.ntt_batch_stats(self._b, out)
+        return {"graph_replays": out[0], "tuned": out[1], "last_lanes": out[2], "compositions": out[3]}
+
+    @property
+    def graph_replays(self) -> int:
+        """Runs of this batch object served from a captured CUDA graph."""
+        return self.stats()["graph_replays"]

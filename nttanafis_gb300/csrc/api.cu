@@ -28,6 +28,13 @@ typedef unsigned __int128 u128;
 
 static thread_local std::string g_error;
 static std::atomic<uint64_t> g_launches{0};
+// Set while this thread captures a batch into a CUDA graph: the captured launches
+// are counted when the graph runs, not when it is recorded.
+static thread_local bool t_capturing = false;
+
+static void note_launches(uint64_t n) {
+    if (!t_capturing) g_launches += n;
+}
 
 // Optional per-kernel timing: when set, an event is recorded on the launching
 // stream before the first kernel of a call and after every kernel.
@@ -521,22 +528,22 @@ static bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq
     ta.wide = g0.wide;
     const bool sign = g0.sign != 0;
     if (!g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
-        g_launches += 1;
+        note_launches(1);
         return cuda_ok(launch_small_fused(ta, cp, sq, st), "batched fused product launch");
     }
     if (g0.log_t <= kMaxBlockLog) {
-        g_launches += 1;
+        note_launches(1);
         if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return false;
     } else {
         ta.log_r = g0.log_t / 2;
         ta.log_c = g0.log_t - ta.log_r;
-        g_launches += 3;
+        note_launches(3);
         if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch") ||
             !cuda_ok(launch_rows(ta, sq, st), "batched row pass launch") ||
             !cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch"))
             return false;
     }
-    g_launches += 1;
+    note_launches(1);
     if (g0.conv)
         return cuda_ok(launch_crt_conv_batch(descs, n, max_len, g0.log_t, cp, st), "batched CRT launch");
     return cuda_ok(launch_crt_mul_batch(descs, n, (int)((max_len + kCrtTile - 1) / kCrtTile), g0.log_t, cp, st),
@@ -564,14 +571,14 @@ static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_
     const u64 chunk = g.split_chunk();
     for (u64 first = 0; first < g.blocks; first += chunk) {
         const u64 count = std::min(chunk, g.blocks - first);
-        g_launches += 1;
+        note_launches(1);
         if (!cuda_ok(launch_split_descs(descs, first, count, lng, L, sht, S, g.block, d_dst, odd, arena, member, spec,
                                         st),
                      "split descriptors") ||
             !run_members(descs, (int)count, g, false, g.block + S, st))
             return false;
     }
-    g_launches += 1;
+    note_launches(1);
     return cuda_ok(launch_add_limbs(d_dst, odd, g.out_len, flags, st), "block sum");
 }
 
@@ -588,7 +595,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         return ok;
     }
     if (g.conv && g.schoolbook) {
-        g_launches += 1;
+        note_launches(1);
         const bool ok = cuda_ok(launch_conv_schoolbook(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst,
                                                        (int)g.stride, g.sign != 0, st),
                                 "conv schoolbook launch");
@@ -619,21 +626,21 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         ta.dst = d_dst;
         ta.out_len = g.out_len;
-        g_launches += 1;
+        note_launches(1);
         const bool ok = cuda_ok(launch_small_fused(ta, cp, square, st), "fused product launch");
         mark(st);
         return ok;
     }
     if (g.log_t <= kMaxBlockLog) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
-        g_launches += 1;
+        note_launches(1);
         if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
         mark(st);
     } else {
         ta.log_r = g.log_t / 2;
         ta.log_c = g.log_t - ta.log_r;
         if (b_ready && !square) {
-            g_launches += 1;
+            note_launches(1);
             ta.op_count = 1;
             if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) return false;
             if (!cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
@@ -644,7 +651,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         } else if (!cuda_ok(launch_fwd_cols(ta, square, sign, st), "column pass launch")) {
             return false;
         }
-        g_launches += 3;
+        note_launches(3);
         mark(st);
         if (!cuda_ok(launch_rows(ta, square, st), "row pass launch")) return false;
         mark(st);
@@ -652,12 +659,12 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         mark(st);
     }
     if (g.conv) {
-        g_launches += 1;
+        note_launches(1);
         const bool ok = cuda_ok(launch_crt_conv(ta.spec, g.log_t, g.conv_len, d_dst, sign, cp, st), "CRT launch");
         mark(st);
         return ok;
     }
-    g_launches += 1;
+    note_launches(1);
     return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst,
                                   (uint8_t*)scratch + spec_bytes, cp, st, mark),
                    "CRT launch");
@@ -1067,6 +1074,43 @@ int ntt_timing_stop(float* ms, int capacity) {
 // transform class (kind, length, primes, sign, square); each class runs as one launch of
 // every kernel of its path, with the member index in the last grid dimension.
 
+// Scheduling of a batch run. Classes are independent: they run on 1, 2 or 4
+// streams of the batch object (lanes, forked from and joined back into the
+// caller's stream), so that one class's kernel tails overlap the next class's
+// kernels. Which lane count is fastest depends on the composition (the sequence
+// of classes with their member counts and longest results): many small classes
+// gain from concurrency, a few large ones fill the GPU alone and lose L2 locality
+// when they share it. So a composition that repeats is tuned on its own runs: its
+// second to seventh runs try each lane count twice, timed by CUDA events on the
+// caller's stream, and the fastest is captured into a CUDA graph that serves every
+// later run (the members' pointers and lengths live in the device descriptors,
+// uploaded before every run, so one graph serves every batch of the composition).
+// A composition seen once runs with lanes picked from its size.
+constexpr int kBatchLanes = 4;
+constexpr size_t kBatchCompositions = 32;  // remembered per batch object
+constexpr int kLaneChoices[3] = {4, 2, 1};
+constexpr int kTrials = 6;                 // each lane count twice
+
+struct Composition {
+    uint64_t seen = 0;
+    uint64_t used = 0;  // last use, for eviction
+    int trials = 0;     // tuning runs enqueued
+    cudaEvent_t t0[kTrials] = {}, t1[kTrials] = {};
+    int lanes = 0;      // chosen lane count (0: not tuned yet)
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0;  // kernel nodes, counted at every replay
+};
+
+static void release_composition(Composition& c) {
+    for (int i = 0; i < kTrials; ++i) {
+        if (c.t0[i]) cudaEventDestroy(c.t0[i]);
+        if (c.t1[i]) cudaEventDestroy(c.t1[i]);
+        c.t0[i] = c.t1[i] = nullptr;
+    }
+    if (c.exec) cudaGraphExecDestroy(c.exec);
+    c.exec = nullptr;
+}
+
 struct ntt_batch {
     int device = 0;
     DeviceBuf arena;  // residues and carry flags of every member
@@ -1075,14 +1119,41 @@ struct ntt_batch {
     size_t host_cap = 0;
     cudaEvent_t staged = nullptr;  // the last descriptor upload has been read
     bool pending = false;
+    cudaStream_t lane[kBatchLanes] = {};
+    cudaEvent_t lane_done[kBatchLanes] = {};
+    cudaEvent_t fork = nullptr;
+    bool graphs = true;
+    int fixed_lanes = 0;  // 1..4 set by the caller, 0: tuned per composition
+    int last_lanes = 0;
+    uint64_t clock = 0;
+    uint64_t replays = 0;
+    uint64_t tuned = 0;
+    std::map<std::vector<uint64_t>, Composition> comps;
 };
+
+static void destroy_batch_events(ntt_batch* b) {
+    for (int i = 0; i < kBatchLanes; ++i) {
+        if (b->lane[i]) cudaStreamDestroy(b->lane[i]);
+        if (b->lane_done[i]) cudaEventDestroy(b->lane_done[i]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->staged) cudaEventDestroy(b->staged);
+    for (auto& kv : b->comps) release_composition(kv.second);
+    b->comps.clear();
+}
 
 ntt_batch* ntt_batch_new(void) {
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return nullptr;
     ntt_batch* b = new ntt_batch();
     b->device = dev;
-    if (!cuda_ok(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate")) {
+    bool ok = cuda_ok(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate") &&
+              cuda_ok(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate");
+    for (int i = 0; ok && i < kBatchLanes; ++i)
+        ok = cuda_ok(cudaStreamCreateWithFlags(&b->lane[i], cudaStreamNonBlocking), "cudaStreamCreate") &&
+             cuda_ok(cudaEventCreateWithFlags(&b->lane_done[i], cudaEventDisableTiming), "cudaEventCreate");
+    if (!ok) {
+        destroy_batch_events(b);
         delete b;
         return nullptr;
     }
@@ -1097,8 +1168,30 @@ void ntt_batch_free(ntt_batch* b) {
     b->arena.release();
     b->desc.release();
     if (b->host_desc) cudaFreeHost(b->host_desc);
-    cudaEventDestroy(b->staged);
+    destroy_batch_events(b);
     delete b;
+}
+
+int ntt_batch_set_graphs(ntt_batch* b, int on) {
+    if (!b) return -1;
+    const int prev = b->graphs ? 1 : 0;
+    if (on == 0 || on == 1) b->graphs = on == 1;
+    return prev;
+}
+
+int ntt_batch_set_lanes(ntt_batch* b, int lanes) {
+    if (!b) return -1;
+    const int prev = b->fixed_lanes;
+    if (lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4) b->fixed_lanes = lanes;
+    return prev;
+}
+
+void ntt_batch_stats(const ntt_batch* b, uint64_t* out) {
+    if (!out) return;
+    out[0] = b ? b->replays : 0;
+    out[1] = b ? b->tuned : 0;
+    out[2] = b ? (uint64_t)b->last_lanes : 0;
+    out[3] = b ? b->comps.size() : 0;
 }
 
 namespace {
@@ -1108,12 +1201,182 @@ struct Member {
     bool square;
     u64 offset;  // bytes into the arena
 };
+
+// Members [k, end) of one transform class, in descriptor order.
+struct BatchClass {
+    size_t k, end;
+    Geom g;
+    bool square;
+    u64 max_len;
+    double work;  // butterfly levels of the class
+};
 }  // namespace
+
+// Lanes of a composition that is not tuned: concurrency for small batches (the
+// lane count that the tuner picks for 64 to 1,024 mixed products of 256..65,536
+// limbs), one stream for large ones.
+static int default_lanes(const std::vector<BatchClass>& cls) {
+    double work = 0;
+    for (const BatchClass& c : cls) work += c.work;
+    // about 1.5 ms of transforms on one GB300
+    return work < 2.0e9 ? (work < 2.5e8 ? 4 : 2) : 1;
+}
+
+// Enqueues every class on `st`, spread over `lanes` streams. Returns false on a
+// launch failure.
+static bool enqueue_classes(ntt_batch* b, const std::vector<BatchClass>& cls, const ProductDesc* dev_desc,
+                            cudaStream_t st, int lanes) {
+    lanes = (int)std::min<size_t>(cls.size(), (size_t)lanes);
+    b->last_lanes = lanes;
+    if (lanes <= 1) {
+        for (const BatchClass& c : cls)
+            if (!run_members(dev_desc + c.k, (int)(c.end - c.k), c.g, c.square, c.max_len, st)) return false;
+        return true;
+    }
+    if (!cuda_ok(cudaEventRecord(b->fork, st), "cudaEventRecord")) return false;
+    for (int i = 0; i < lanes; ++i)
+        if (!cuda_ok(cudaStreamWaitEvent(b->lane[i], b->fork, 0), "cudaStreamWaitEvent")) return false;
+    // Largest classes first, each to the lane with the least work so far.
+    std::vector<size_t> order(cls.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cls[x].work > cls[y].work; });
+    double load[kBatchLanes] = {};
+    for (size_t i : order) {
+        int lane = 0;
+        for (int l = 1; l < lanes; ++l)
+            if (load[l] < load[lane]) lane = l;
+        load[lane] += cls[i].work;
+        const BatchClass& c = cls[i];
+        if (!run_members(dev_desc + c.k, (int)(c.end - c.k), c.g, c.square, c.max_len, b->lane[lane])) return false;
+    }
+    for (int i = 0; i < lanes; ++i)
+        if (!cuda_ok(cudaEventRecord(b->lane_done[i], b->lane[i]), "cudaEventRecord") ||
+            !cuda_ok(cudaStreamWaitEvent(st, b->lane_done[i], 0), "cudaStreamWaitEvent"))
+            return false;
+    return true;
+}
+
+// Kernel nodes of a captured graph.
+static uint64_t graph_kernels(cudaGraph_t graph) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(graph, nullptr, &n) != cudaSuccess || n == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(graph, nodes.data(), &n) != cudaSuccess) return 0;
+    uint64_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+// Captures the classes with `lanes` into the composition's graph and runs it.
+static bool capture_and_run(ntt_batch* b, Composition& e, const std::vector<BatchClass>& cls,
+                            const ProductDesc* dev_desc, cudaStream_t st, int lanes) {
+    // Every table and constant the classes need exists by now (the first run built
+    // them), so the capture records launches only.
+    if (!cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture")) return false;
+    t_capturing = true;
+    const bool recorded = enqueue_classes(b, cls, dev_desc, st, lanes);
+    t_capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t end = cudaStreamEndCapture(st, &graph);
+    bool ok = recorded && cuda_ok(end, "cudaStreamEndCapture");
+    if (ok) {
+        e.kernels = graph_kernels(graph);
+        ok = cuda_ok(cudaGraphInstantiate(&e.exec, graph, 0), "cudaGraphInstantiate");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+        e.exec = nullptr;
+        return false;
+    }
+    if (!cuda_ok(cudaGraphLaunch(e.exec, st), "cudaGraphLaunch")) return false;
+    note_launches(e.kernels);
+    ++b->replays;
+    return true;
+}
+
+// Runs the classes of one batch run (see the scheduling note above). Streams that
+// cannot be captured (the legacy default stream) and batches with graphs off run
+// directly, tuned lanes still applying when graphs are off.
+static bool run_classes(ntt_batch* b, const std::vector<BatchClass>& cls, const ProductDesc* dev_desc,
+                        cudaStream_t st) {
+    const bool capturable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+    std::vector<uint64_t> sig;
+    sig.reserve(4 * cls.size() + 2);
+    sig.push_back((uint64_t)(uintptr_t)dev_desc);
+    sig.push_back((uint64_t)b->fixed_lanes);
+    for (const BatchClass& c : cls) {
+        sig.push_back(c.end - c.k);
+        sig.push_back(c.max_len);
+        sig.push_back(((uint64_t)c.g.log_t << 32) | ((uint64_t)c.g.np << 16) | ((uint64_t)c.g.conv << 3) |
+                      ((uint64_t)c.g.wide << 2) | ((uint64_t)(c.g.sign != 0) << 1) | (c.square ? 1u : 0u));
+        sig.push_back(c.g.stride);
+    }
+    auto found = b->comps.find(sig);
+    if (found == b->comps.end()) {
+        if (b->comps.size() >= kBatchCompositions) {  // forget the least recently used composition
+            auto old = b->comps.begin();
+            for (auto it = b->comps.begin(); it != b->comps.end(); ++it)
+                if (it->second.used < old->second.used) old = it;
+            if (!cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize")) return false;
+            release_composition(old->second);
+            b->comps.erase(old);
+        }
+        found = b->comps.emplace(sig, Composition()).first;
+    }
+    Composition& e = found->second;
+    e.used = ++b->clock;
+    ++e.seen;
+    const int fixed = b->fixed_lanes;
+    if (!capturable) return enqueue_classes(b, cls, dev_desc, st, fixed ? fixed : (e.lanes ? e.lanes : default_lanes(cls)));
+    if (e.exec && b->graphs) {
+        if (!cuda_ok(cudaGraphLaunch(e.exec, st), "cudaGraphLaunch")) return false;
+        note_launches(e.kernels);
+        ++b->replays;
+        return true;
+    }
+    if (fixed) {  // the caller's lane count: no tuning, a graph from the second run
+        if (e.seen >= 2 && b->graphs) return capture_and_run(b, e, cls, dev_desc, st, fixed);
+        return enqueue_classes(b, cls, dev_desc, st, fixed);
+    }
+    if (e.seen < 2) return enqueue_classes(b, cls, dev_desc, st, e.lanes ? e.lanes : default_lanes(cls));
+    if (e.lanes == 0 && e.trials < kTrials) {  // a timed tuning run
+        const int i = e.trials++;
+        if (!e.t0[i] && (!cuda_ok(cudaEventCreate(&e.t0[i]), "cudaEventCreate") ||
+                         !cuda_ok(cudaEventCreate(&e.t1[i]), "cudaEventCreate")))
+            return false;
+        return cuda_ok(cudaEventRecord(e.t0[i], st), "cudaEventRecord") &&
+               enqueue_classes(b, cls, dev_desc, st, kLaneChoices[i % 3]) &&
+               cuda_ok(cudaEventRecord(e.t1[i], st), "cudaEventRecord");
+    }
+    if (e.lanes == 0) {  // every trial is enqueued: pick the fastest lane count
+        float best[3] = {1e30f, 1e30f, 1e30f};
+        if (!cuda_ok(cudaEventSynchronize(e.t1[kTrials - 1]), "cudaEventSynchronize")) return false;
+        for (int i = 0; i < kTrials; ++i) {
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, e.t0[i], e.t1[i]) == cudaSuccess) best[i % 3] = std::min(best[i % 3], ms);
+        }
+        int pick = 0;
+        for (int j = 1; j < 3; ++j)
+            if (best[j] < best[pick]) pick = j;
+        e.lanes = kLaneChoices[pick];
+        ++b->tuned;
+    }
+    if (!b->graphs) return enqueue_classes(b, cls, dev_desc, st, e.lanes);
+    return capture_and_run(b, e, cls, dev_desc, st, e.lanes);
+}
 
 uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count, void* stream) {
     if (!b || (!reqs && count)) return fail("null argument");
     if (!cuda_ok(cudaSetDevice(b->device), "cudaSetDevice")) return 0;
     cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (st && st != cudaStreamLegacy && st != cudaStreamPerThread &&
+        (!cuda_ok(cudaStreamIsCapturing(st, &cap), "cudaStreamIsCapturing") || cap != cudaStreamCaptureStatusNone))
+        return fail("the stream is being captured: a batch stages its descriptors from the host on every run "
+                    "and captures its own graphs");
     // Plan every member first: a batch with an inadmissible member launches nothing.
     std::vector<Member> members;
     members.reserve(count);
@@ -1187,7 +1450,10 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         return 0;
     b->pending = true;
     const ProductDesc* dev_desc = (const ProductDesc*)b->desc.ptr;
+    // Schoolbook convolutions take their operands as launch arguments: they run
+    // directly. Every other class goes through the descriptors.
     constexpr size_t kMaxLaunchMembers = 16384;  // 2 * members fits gridDim.z
+    std::vector<BatchClass> classes;
     size_t k = 0;
     while (k < members.size()) {
         const Geom& g0 = members[k].g;
@@ -1197,12 +1463,10 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
                members[end].g.np == g0.np && members[end].g.sign == g0.sign &&
                members[end].square == members[k].square)
             ++end;
-        const bool sq = members[k].square;
-        const int n = (int)(end - k);
         if (g0.conv && g0.schoolbook) {
             for (size_t i = k; i < end; ++i) {
                 const ProductDesc& d = b->host_desc[i];
-                g_launches += 1;
+                note_launches(1);
                 if (!cuda_ok(launch_conv_schoolbook(d.a, d.la, d.b, d.lb, d.dst, (int)d.stride, g0.sign != 0, st),
                              "conv schoolbook launch"))
                     return 0;
@@ -1210,13 +1474,26 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
             k = end;
             continue;
         }
-        u64 max_len = 0;
+        BatchClass c;
+        c.k = k;
+        c.end = end;
+        c.g = g0;
+        c.square = members[k].square;
+        c.max_len = 0;
         for (size_t i = k; i < end; ++i)
-            max_len = std::max(max_len, g0.conv ? members[i].g.conv_len : members[i].g.out_len);
-        if (!run_members(dev_desc + k, n, g0, sq, max_len, st)) return 0;
+            c.max_len = std::max(c.max_len, g0.conv ? members[i].g.conv_len : members[i].g.out_len);
+        c.work = (double)(end - k) * g0.np * (double)((u64)1 << g0.log_t) * g0.log_t;
+        classes.push_back(c);
         k = end;
     }
-    return 1;
+    if (classes.empty()) return 1;
+    // Tables and constants of every class before any capture.
+    for (const BatchClass& c : classes) {
+        PrimeSet ps;
+        CrtParams cp;
+        if (!prepare_params(c.g, ps, cp)) return 0;
+    }
+    return run_classes(b, classes, dev_desc, st) ? 1 : 0;
 }
 
 uint32_t ntt_lookback_timeouts(void) { return lookback_timeouts(); }

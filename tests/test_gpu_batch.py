@@ -101,3 +101,58 @@ def test_inadmissible_member_launches_nothing(gpu):
     torch.cuda.synchronize()
     assert bool((z == 0).all())
     batch.close()
+
+
+def check_batch(gpu, torch, batch, shapes, st):
+    reqs, keep = run_batch(gpu, torch, shapes)
+    assert batch.run(reqs, st), gpu.last_error()
+    st.synchronize()
+    for s, a, b, dst in keep:
+        host = dst.cpu().numpy().view(np.uint64)
+        assert host[-1] == MASK, s
+        assert np.array_equal(host[:-1], expected(s, a, b)), s
+
+
+def test_tuned_composition_replays_from_a_graph(gpu):
+    # A repeated composition: run 1 direct, runs 2-7 time the lane counts, run 8
+    # captures the fastest into a CUDA graph, later runs replay it with new
+    # operands (new descriptors). Every run matches the oracle.
+    import torch
+
+    st = torch.cuda.Stream()
+    lengths = [("mul", 700, 300), ("sqr", 1500, 1500), ("mul", 9000, 7000), ("conv", 3000, 2000),
+               ("mul", 40000, 5000), ("sqr", 20000, 20000), ("mul", 100, 90), ("conv", 50000, 1000)]
+    batch = gpu.GpuBatch()
+    for run in range(9):
+        shapes = [Shape(k, la, lb, 100 * run + 2 * i + 1, 100 * run + 2 * i + 2, bits=32, signed=True)
+                  for i, (k, la, lb) in enumerate(lengths)]
+        check_batch(gpu, torch, batch, shapes, st)
+        stats = batch.stats()
+        assert stats["tuned"] == (1 if run >= 7 else 0), (run, stats)
+        assert stats["graph_replays"] == max(0, run - 6), (run, stats)
+    assert batch.stats()["compositions"] == 1
+    # graphs off: the tuned lane count, enqueued directly
+    batch.set_graphs(False)
+    shapes = [Shape(k, la, lb, 2 * i + 1, 2 * i + 2, bits=32, signed=True) for i, (k, la, lb) in enumerate(lengths)]
+    check_batch(gpu, torch, batch, shapes, st)
+    assert batch.stats()["graph_replays"] == 2
+    batch.close()
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_fixed_lanes_capture_at_the_second_run(gpu, lanes):
+    import torch
+
+    st = torch.cuda.Stream()
+    batch = gpu.GpuBatch()
+    assert batch.set_lanes(lanes) == 0
+    for run in range(3):
+        shapes = [Shape("mul", 5000, 4000, 7 + run, 8), Shape("sqr", 300, 300, 9, 9), Shape("mul", 20, 33, 1, run),
+                  Shape("conv", 4000, 4000, 3, 4 + run, bits=16)]
+        check_batch(gpu, torch, batch, shapes, st)
+        assert batch.stats()["graph_replays"] == run
+        assert batch.stats()["tuned"] == 0
+    # the legacy default stream runs directly
+    check_batch(gpu, torch, batch, shapes, torch.cuda.default_stream())
+    assert batch.stats()["graph_replays"] == 2
+    batch.close()
