@@ -486,6 +486,8 @@ def run_gpu(args) -> None:
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     lib = ntt.library()
+    # Four-step split per transform length, measured on this GPU (a fraction of a second).
+    splits = {} if args.no_tune else ntt.tune_splits(14, 23, reps=3, stream=torch.cuda.current_stream(dev))
 
     per_step_in = 8 * (LA + LB)
     nsets = max(2, -(-2 * L2_BYTES // per_step_in))  # rotating inputs larger than L2
@@ -648,6 +650,7 @@ def run_gpu(args) -> None:
         "config": {"workload": WORKLOAD, "la": LA, "lb": LB, "primes": plan.primes,
                    "log_transform": plan.log_transform, "parallelism": f"replicas x{world}",
                    "streams": nstreams, "one_stream_products_per_s": 1000.0 / one_stream_ms,
+                   "four_step_splits": {f"2^{t}": f"2^{r} x 2^{t - r}" for t, r in splits.items()},
                    "l2": f"inputs larger than L2: {nsets} rotating operand pairs ({nsets * per_step_in >> 20} MiB)"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": per_step_in,
                 "d2h_bytes_per_step": 8 * (LA + LB), "api": "ntt_mul_workspace_mul (host pointers, pinned)",
@@ -702,6 +705,7 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-configuration section")
     ap.add_argument("--no-served", action="store_true", help="skip the served-configuration section")
     ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration timings")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default four-step splits (no tuning run)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--streams", type=int, default=2, help="streams (and workspaces) the timed products alternate on")
     ap.add_argument("--e2e-threads", type=int, default=4, help="host threads making the host-pointer calls")

@@ -267,6 +267,22 @@ uint8_t ntt_field_evaluate_device(uint64_t modulus, uint64_t* d_out, const uint6
 uint8_t ntt_crt_pair_combine_device(uint64_t first, uint64_t second, int64_t* d_out, const uint64_t* d_first,
                                     const uint64_t* d_second, size_t n, void* stream);
 
+/* Four-step split T = R * C of the lazy transform lengths 2^14..2^23, process-wide:
+ * ntt_split_set makes R = 2^log_r for transforms of 2^log_t points (0 restores the
+ * default floor(log_t / 2)) and returns the previous log_r, or -1 when log_t has no
+ * choice of split or log_r is outside the range that ntt_split_range reports
+ * (columns 2^7..2^11, rows 2^7..2^12). ntt_split_get returns the log_r in use (0
+ * for lengths without a four-step split). The split changes speed, never results.
+ * ntt_tune_splits times every split of each length in [min_log_t, max_log_t] on
+ * balanced products that fill the transform (`reps` products per timing, best of
+ * two) on `stream` and keeps the fastest when it beats the default by 2%; it
+ * synchronizes `stream` and allocates its operands for the call. No reference
+ * counterpart: the reference fixes its geometry in Geometry::select. */
+int ntt_split_set(int log_t, int log_r);
+int ntt_split_get(int log_t);
+int ntt_split_range(int log_t, int* lo, int* hi);
+uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream);
+
 /* Look-back waits of the CRT carry scan that gave up since the library was loaded
  * (each wait is bounded; a nonzero count means a result may be wrong). Synchronizes
  * the device. */

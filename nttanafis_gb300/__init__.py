@@ -10,6 +10,12 @@ from .api import (  # noqa: F401
     Request,
     MulPlan,
     butterfly_rate,
+    get_split,
+    load_splits,
+    save_splits,
+    set_split,
+    split_range,
+    tune_splits,
     exported_symbols,
     kernel_launches,
     last_error,

@@ -105,6 +105,10 @@ _SIGNATURES = [
     ("ntt_timing_start", ctypes.c_int, [ctypes.c_int]),
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_lookback_timeouts", ctypes.c_uint32, []),
+    ("ntt_split_set", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    ("ntt_split_get", ctypes.c_int, [ctypes.c_int]),
+    ("ntt_split_range", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    ("ntt_tune_splits", ctypes.c_uint8, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     ("ntt_probe_butterflies", ctypes.c_uint8, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("ntt_field_check", ctypes.c_int, [ctypes.c_uint64]),
     ("ntt_field_mul_method", ctypes.c_int, [ctypes.c_int]),
@@ -166,6 +170,56 @@ def kernel_launches() -> int:
 def lookback_timeouts() -> int:
     """Bounded look-back waits of the CRT carry scan that gave up (expected 0)."""
     return int(library().ntt_lookback_timeouts())
+
+
+def split_range(log_t: int) -> Optional[tuple[int, int]]:
+    """(lowest, highest) log2 R of the four-step split of 2^log_t points, or None
+    when that length has no choice of split."""
+    lo, hi = ctypes.c_int(0), ctypes.c_int(0)
+    if not library().ntt_split_range(log_t, ctypes.byref(lo), ctypes.byref(hi)):
+        return None
+    return lo.value, hi.value
+
+
+def get_split(log_t: int) -> int:
+    """log2 R of the four-step split in use for 2^log_t points (0: no four-step form)."""
+    return int(library().ntt_split_get(log_t))
+
+
+def set_split(log_t: int, log_r: int) -> int:
+    """Sets log2 R for 2^log_t points (0: the default); returns the previous one."""
+    prev = int(library().ntt_split_set(log_t, log_r))
+    if prev < 0:
+        raise ValueError(f"no split 2^{log_r} for transforms of 2^{log_t} points")
+    return prev
+
+
+def tune_splits(min_log_t: int = 14, max_log_t: int = 23, reps: int = 5, stream=None) -> dict:
+    """Times every four-step split of each transform length on the current GPU and
+    keeps the fastest (see ntt_tune_splits); returns {log_t: log_r} in use after it."""
+    if not library().ntt_tune_splits(min_log_t, max_log_t, reps, _stream_handle(stream)):
+        raise RuntimeError(last_error())
+    return {t: get_split(t) for t in range(max(min_log_t, 14), min(max_log_t, 23) + 1)}
+
+
+def save_splits(path) -> None:
+    """Writes the splits in use to a JSON file (tuning results for the next run)."""
+    import json
+
+    data = {str(t): get_split(t) for t in range(14, 24) if split_range(t)}
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1)
+
+
+def load_splits(path) -> dict:
+    """Applies splits saved by save_splits; returns them."""
+    import json
+
+    with open(path) as f:
+        data = {int(k): int(v) for k, v in json.load(f).items()}
+    for t, r in data.items():
+        set_split(t, r)
+    return data
 
 
 def butterfly_rate(blocks: int = 152 * 8, iters: int = 2000) -> float:

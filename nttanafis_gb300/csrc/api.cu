@@ -331,7 +331,7 @@ struct StepTables {
 
 static std::mutex g_table_mutex;
 static std::map<std::pair<int, u32>, PrimeTables> g_prime_tables;
-static std::map<std::tuple<int, u32, int>, StepTables> g_step_tables;
+static std::map<std::tuple<int, u32, int, int>, StepTables> g_step_tables;
 static std::map<int, bool> g_device_ready;
 
 static uint2 shoup_pair(u32 w, u32 p) { return make_uint2(w, (u32)(((u64)w << 32) / p)); }
@@ -392,8 +392,8 @@ static cudaStream_t table_stream(int dev) {
 // Root tables of one transform length: the inverse scale and, for the four-step
 // sizes, the forward and inverse twiddle factors in the layouts the column and row
 // passes read (launch.h describes them), built by a kernel from the squares of w.
-static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
-    auto key = std::make_tuple(dev, p, log_t);
+static bool step_tables(int dev, u32 p, int log_t, int log_r, StepTables& out) {
+    auto key = std::make_tuple(dev, p, log_t, log_r);
     auto it = g_step_tables.find(key);
     if (it != g_step_tables.end()) { out = it->second; return true; }
     const u32 g = generator(p);
@@ -408,8 +408,8 @@ static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
         memset(&b, 0, sizeof(b));
         b.p = p;
         b.log_t = log_t;
-        b.log_r = log_t / 2;
-        b.log_c = log_t - b.log_r;
+        b.log_r = log_r;
+        b.log_c = log_t - log_r;
         u32 x = w, ix = iw;
         for (int i = 0; i <= log_t; ++i) {
             b.fwd_pow[i] = shoup_pair(x, p);
@@ -419,7 +419,7 @@ static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
         }
         b.scale = t.scale;
         u64 n[4];
-        step_table_sizes(log_t, n);
+        step_table_sizes(log_t, log_r, n);
         uint2** dst[4] = {&t.f_a, &t.f_b, &t.i_lo, &t.i_hi};
         for (int i = 0; i < 4; ++i)
             if (!cuda_ok(cudaMalloc((void**)dst[i], n[i] * sizeof(uint2)), "cudaMalloc(table)")) return false;
@@ -437,14 +437,35 @@ static bool step_tables(int dev, u32 p, int log_t, StepTables& out) {
     return true;
 }
 
-// Fills the kernel constants of a plan; builds missing tables on the current device.
-static std::map<std::tuple<int, int, int>, std::pair<PrimeSet, CrtParams>> g_param_cache;
+// Four-step split of the lazy transforms: log2 R for each length 2^log_t, 0 for
+// the default floor(log_t / 2). Set by ntt_split_set, e.g. from ntt_tune_splits.
+static std::atomic<int> g_split[kMaxLogT + 1];
 
-static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
+// Range of log2 R with column and row kernels for a lazy transform of 2^log_t
+// points (columns 2^7..2^11, rows 2^7..2^12); false when the length has no
+// four-step form or is one of the wide lengths.
+static bool split_range(int log_t, int& lo, int& hi) {
+    if (log_t <= kMaxBlockLog || log_t > 23) return false;
+    lo = std::max(7, log_t - 12);
+    hi = std::min(11, log_t - 7);
+    return lo <= hi;
+}
+
+static int four_step_log_r(const Geom& g) {
+    if (g.log_t <= kMaxBlockLog) return 0;
+    const int o = g.wide ? 0 : g_split[g.log_t].load(std::memory_order_relaxed);
+    return o ? o : g.log_t / 2;
+}
+
+// Fills the kernel constants of a plan whose four-step split is R = 2^log_r (0 for
+// the one-CTA lengths); builds missing tables on the current device.
+static std::map<std::tuple<int, int, int, int>, std::pair<PrimeSet, CrtParams>> g_param_cache;
+
+static bool prepare_params(const Geom& g, int log_r, PrimeSet& ps, CrtParams& cp) {
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
     std::lock_guard<std::mutex> lock(g_table_mutex);
-    const auto key = std::make_tuple(dev, g.log_t, g.np);
+    const auto key = std::make_tuple(dev, g.log_t, g.np, log_r);
     auto hit = g_param_cache.find(key);
     if (hit != g_param_cache.end()) {
         ps = hit->second.first;
@@ -467,7 +488,7 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
         const u32 p = g.primes[i];
         PrimeTables pt;
         StepTables st;
-        if (!prime_tables(dev, p, pt) || !step_tables(dev, p, g.log_t, st)) return false;
+        if (!prime_tables(dev, p, pt) || !step_tables(dev, p, g.log_t, log_r, st)) return false;
         PrimeParams& pp = ps.pr[i];
         pp.p = p;
         u32 pinv = 1;  // p^-1 mod 2^32 by Newton's iteration (bits double each step)
@@ -510,6 +531,10 @@ static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
     return true;
 }
 
+static bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp) {
+    return prepare_params(g, four_step_log_r(g), ps, cp);
+}
+
 // ---------------------------------------------------------------------------------
 // Execution on device pointers
 
@@ -520,7 +545,8 @@ static bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq
     TransformArgs ta;
     memset(&ta, 0, sizeof(ta));
     CrtParams cp;
-    if (!prepare_params(g0, ta.ps, cp)) return false;
+    const int log_r = four_step_log_r(g0);
+    if (!prepare_params(g0, log_r, ta.ps, cp)) return false;
     ta.batch = descs;
     ta.count = n;
     ta.np = g0.np;
@@ -535,7 +561,7 @@ static bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq
         note_launches(1);
         if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return false;
     } else {
-        ta.log_r = g0.log_t / 2;
+        ta.log_r = log_r;
         ta.log_c = g0.log_t - ta.log_r;
         note_launches(3);
         if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch") ||
@@ -605,7 +631,8 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
     TransformArgs ta;
     memset(&ta, 0, sizeof(ta));
     CrtParams cp;
-    if (!prepare_params(g, ta.ps, cp)) return false;
+    const int log_r = four_step_log_r(g);
+    if (!prepare_params(g, log_r, ta.ps, cp)) return false;
     ta.a = d_a;
     ta.b = square ? d_a : d_b;
     ta.la = g.la;
@@ -637,7 +664,7 @@ static bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, 
         if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
         mark(st);
     } else {
-        ta.log_r = g.log_t / 2;
+        ta.log_r = log_r;
         ta.log_c = g.log_t - ta.log_r;
         if (b_ready && !square) {
             note_launches(1);
@@ -1494,6 +1521,82 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         if (!prepare_params(c.g, ps, cp)) return 0;
     }
     return run_classes(b, classes, dev_desc, st) ? 1 : 0;
+}
+
+int ntt_split_set(int log_t, int log_r) {
+    int lo = 0, hi = 0;
+    if (!split_range(log_t, lo, hi) || (log_r != 0 && (log_r < lo || log_r > hi))) return -1;
+    const int prev = g_split[log_t].exchange(log_r == log_t / 2 ? 0 : log_r);
+    return prev ? prev : log_t / 2;
+}
+
+int ntt_split_get(int log_t) {
+    int lo = 0, hi = 0;
+    if (!split_range(log_t, lo, hi)) return 0;
+    const int o = g_split[log_t].load();
+    return o ? o : log_t / 2;
+}
+
+int ntt_split_range(int log_t, int* lo, int* hi) {
+    int l = 0, h = 0;
+    if (!split_range(log_t, l, h)) return 0;
+    if (lo) *lo = l;
+    if (hi) *hi = h;
+    return 1;
+}
+
+uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream) {
+    min_log_t = std::max(min_log_t, kMaxBlockLog + 1);
+    max_log_t = std::min(max_log_t, 23);
+    if (min_log_t > max_log_t) return 1;
+    reps = std::max(1, reps);
+    cudaStream_t st = (cudaStream_t)stream;
+    const u64 half = (u64)1 << (max_log_t - 1);
+    u64 *a = nullptr, *b = nullptr, *dst = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ntt_mul_workspace* ws = ntt_mul_workspace_new();
+    bool ok = ws && cuda_ok(cudaMalloc(&a, half * 8), "cudaMalloc") && cuda_ok(cudaMalloc(&b, half * 8), "cudaMalloc") &&
+              cuda_ok(cudaMalloc(&dst, 2 * half * 8), "cudaMalloc") &&
+              cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") && cuda_ok(cudaEventCreate(&e1), "cudaEventCreate") &&
+              cuda_ok(cudaMemsetAsync(a, 0xA5, half * 8, st), "cudaMemset") &&
+              cuda_ok(cudaMemsetAsync(b, 0x3C, half * 8, st), "cudaMemset");
+    for (int log_t = min_log_t; ok && log_t <= max_log_t; ++log_t) {
+        int lo = 0, hi = 0;
+        if (!split_range(log_t, lo, hi) || lo == hi) continue;
+        // operands of 2^(log_t - 1) limbs: the product fills the transform
+        const u64 n = (u64)1 << (log_t - 1);
+        float best = 1e30f, standard = 1e30f;
+        int pick = log_t / 2;
+        for (int r = lo; ok && r <= hi; ++r) {
+            g_split[log_t].store(r == log_t / 2 ? 0 : r);
+            ok = ntt_mul_workspace_mul_device(ws, dst, 2 * n, a, n, b, n, st) == 1;  // tables, warm-up
+            float ms = 1e30f;
+            for (int round = 0; ok && round < 2; ++round) {
+                ok = cuda_ok(cudaEventRecord(e0, st), "cudaEventRecord");
+                for (int i = 0; ok && i < reps; ++i) ok = ntt_mul_workspace_mul_device(ws, dst, 2 * n, a, n, b, n, st) == 1;
+                float t = 0;
+                ok = ok && cuda_ok(cudaEventRecord(e1, st), "cudaEventRecord") &&
+                     cuda_ok(cudaEventSynchronize(e1), "cudaEventSynchronize") &&
+                     cuda_ok(cudaEventElapsedTime(&t, e0, e1), "cudaEventElapsedTime");
+                ms = std::min(ms, t / reps);
+            }
+            if (r == log_t / 2) standard = ms;
+            if (ms < best) {
+                best = ms;
+                pick = r;
+            }
+        }
+        // another split only when it is at least 2% faster than the default
+        if (!(best < 0.98f * standard)) pick = log_t / 2;
+        g_split[log_t].store(pick == log_t / 2 ? 0 : pick);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (ws) ntt_mul_workspace_free(ws);
+    if (a) cudaFree(a);
+    if (b) cudaFree(b);
+    if (dst) cudaFree(dst);
+    return ok ? 1 : 0;
 }
 
 uint32_t ntt_lookback_timeouts(void) { return lookback_timeouts(); }

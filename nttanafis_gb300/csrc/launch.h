@@ -137,9 +137,10 @@ struct StepTableBuild {
     uint2 scale;                  // inverse scale folded into i4_hi
     uint2 *f4_a, *f4_b, *i4_lo, *i4_hi;
 };
-// Entries of the four tables (in the order f4_a, f4_b, i4_lo, i4_hi).
-__host__ __device__ inline void step_table_sizes(int log_t, u64 sizes[4]) {
-    const int log_r = log_t / 2, log_c = log_t - log_r;
+// Entries of the four tables (in the order f4_a, f4_b, i4_lo, i4_hi) of the split
+// T = 2^log_t = R * C, R = 2^log_r.
+__host__ __device__ inline void step_table_sizes(int log_t, int log_r, u64 sizes[4]) {
+    const int log_c = log_t - log_r;
     const u64 R = (u64)1 << log_r, C = (u64)1 << log_c;
     sizes[0] = C << kColLogRS;                     // f4_a: [col][brev(r0)]
     sizes[1] = C * (R >> kColLogRS);               // f4_b: [col][sweep]

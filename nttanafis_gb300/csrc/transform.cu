@@ -476,7 +476,7 @@ __device__ __forceinline__ u32 power_of(const uint2* pow2, u64 e, int bits, u32 
 
 __global__ void __launch_bounds__(256) k_step_tables(const __grid_constant__ StepTableBuild b) {
     u64 n[4];
-    step_table_sizes(b.log_t, n);
+    step_table_sizes(b.log_t, b.log_r, n);
     const u64 mask = ((u64)1 << b.log_t) - 1;
     const int log_sw = b.log_r - kColLogRS, log_nh = b.log_c - kRowTwLoBits;
     const u64 total = n[0] + n[1] + n[2] + n[3];
@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(256) k_step_tables(const __grid_constant__ Ste
 
 cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st) {
     u64 n[4];
-    step_table_sizes(b.log_t, n);
+    step_table_sizes(b.log_t, b.log_r, n);
     const u64 total = n[0] + n[1] + n[2] + n[3];
     const unsigned blocks = (unsigned)std::min<u64>((total + 255) / 256, 152 * 16);
     k_step_tables<<<blocks, 256, 0, st>>>(b);

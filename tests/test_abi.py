@@ -105,3 +105,34 @@ def test_block_split_choice():
     split = ntt.MulPlan.new(2**20, 1024)
     whole_log = (2**20 + 1024 - 1 - 1).bit_length()
     assert split.log_transform < whole_log
+
+
+def test_split_api_ranges_and_validation():
+    # four-step splits: columns 2^7..2^11, rows 2^7..2^12, lazy lengths 2^14..2^23
+    assert ntt.split_range(13) is None and ntt.split_range(24) is None
+    assert ntt.split_range(14) == (7, 7)
+    assert ntt.split_range(21) == (9, 11)
+    assert ntt.split_range(23) == (11, 11)
+    assert ntt.get_split(21) == 10 and ntt.get_split(13) == 0
+    with pytest.raises(ValueError):
+        ntt.set_split(21, 12)
+    with pytest.raises(ValueError):
+        ntt.set_split(13, 6)
+    try:
+        assert ntt.set_split(21, 9) == 10
+        assert ntt.get_split(21) == 9
+    finally:
+        assert ntt.set_split(21, 0) == 9
+    assert ntt.get_split(21) == 10
+
+
+def test_split_file_round_trip(tmp_path):
+    try:
+        ntt.set_split(18, 10)
+        path = tmp_path / "splits.json"
+        ntt.save_splits(path)
+        ntt.set_split(18, 0)
+        assert ntt.load_splits(path)[18] == 10
+        assert ntt.get_split(18) == 10
+    finally:
+        ntt.set_split(18, 0)

@@ -112,6 +112,73 @@ def test_fused_cluster_every_size(ws, log_t):
     assert np.array_equal(gpu_mul(ws, a, c), oracle.mul(a, c)), log_t
 
 
+@pytest.mark.parametrize("log_t", range(15, 24))
+def test_every_four_step_split(ws, gpu, log_t):
+    # every split T = R * C the kernels offer gives the same product and square
+    lo, hi = gpu.split_range(log_t)
+    n = 1 << (log_t - 1)
+    a, b = operand(n, 71 + log_t), operand(n - 5, 72 + log_t)
+    expected = oracle.mul(a, b, THREADS) if log_t <= 20 else None
+    try:
+        for r in range(lo, hi + 1):
+            gpu.set_split(log_t, r)
+            got = gpu_mul(ws, a, b)
+            if expected is not None:
+                assert np.array_equal(got, expected), (log_t, r)
+            else:
+                assert fingerprint_ok(a, b, got), (log_t, r)
+            assert fingerprint_ok(a, a, gpu_sqr(ws, a)), (log_t, r)
+    finally:
+        gpu.set_split(log_t, 0)
+
+
+def test_split_in_batches_and_convolutions(gpu):
+    import torch
+
+    from nttanafis_gb300.workloads import Shape
+
+    # members with T = 2^18
+    shapes = [Shape("mul", 140000, 100000, 1, 2), Shape("sqr", 100000, 100000, 3, 3),
+              Shape("conv", 150000, 100000, 5, 6, bits=32, signed=True)]
+    lo, hi = gpu.split_range(18)
+    batch = gpu.GpuBatch()
+    try:
+        for r in range(lo, hi + 1):
+            gpu.set_split(18, r)
+            reqs, keep = [], []
+            for s in shapes:
+                a_h, b_h = s.operands()
+                a = torch.from_numpy(a_h.view(np.int64)).cuda()
+                b = a if s.kind == "sqr" else torch.from_numpy(b_h.view(np.int64)).cuda()
+                d = torch.empty(s.out_len(), dtype=torch.int64, device="cuda")
+                reqs.append(gpu.Request(d, a, b, "conv" if s.kind == "conv" else "mul", s.max_a, s.max_a, s.signed))
+                keep.append((s, a_h, b_h, d))
+            assert batch.run(reqs), gpu.last_error()
+            torch.cuda.synchronize()
+            for s, a_h, b_h, d in keep:
+                got = d.cpu().numpy().view(np.uint64)
+                if s.kind == "conv":
+                    assert np.array_equal(got, oracle.conv(a_h, b_h, s.max_a, s.max_a, True, THREADS)), r
+                else:
+                    assert fingerprint_ok(a_h, b_h, got), (s, r)
+    finally:
+        gpu.set_split(18, 0)
+        batch.close()
+
+
+def test_split_tuner_keeps_results(ws, gpu):
+    try:
+        chosen = gpu.tune_splits(15, 19, reps=2)
+        for t, r in chosen.items():
+            lo, hi = gpu.split_range(t)
+            assert lo <= r <= hi
+        a, b = operand(1 << 18, 5), operand(1 << 18, 6)
+        assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
+    finally:
+        for t in range(15, 20):
+            gpu.set_split(t, 0)
+
+
 @pytest.mark.parametrize("la,lb", [(4096, 4096), (4097, 4096), (8192, 8191), (8193, 8192), (20000, 13000),
                                    (65536, 65536), (65536, 256), (131072, 131072), (300000, 250000),
                                    (1 << 20, 131072)])
