@@ -442,11 +442,11 @@ static bool step_tables(int dev, u32 p, int log_t, int log_r, StepTables& out) {
 static std::atomic<int> g_split[kMaxLogT + 1];
 
 // Range of log2 R with column and row kernels for a lazy transform of 2^log_t
-// points (columns 2^7..2^11, rows 2^7..2^12); false when the length has no
+// points (columns 2^7..2^11, rows 2^7..2^13); false when the length has no
 // four-step form or is one of the wide lengths.
 static bool split_range(int log_t, int& lo, int& hi) {
     if (log_t <= kMaxBlockLog || log_t > 23) return false;
-    lo = std::max(7, log_t - 12);
+    lo = std::max(7, log_t - 13);
     hi = std::min(11, log_t - 7);
     return lo <= hi;
 }

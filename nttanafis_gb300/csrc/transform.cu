@@ -520,7 +520,7 @@ cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------------
 // Launchers: one instantiation per transform size. The lazy arithmetic covers
-// T <= 2^23 (one-CTA sizes 2^4..2^13, columns 2^7..2^11, rows 2^7..2^12); the wide
+// T <= 2^23 (one-CTA sizes 2^4..2^13, columns 2^7..2^11, rows 2^7..2^13); the wide
 // arithmetic covers T = 2^24, 2^25 (columns 2^12, rows 2^12..2^13).
 
 // Column residues plus the level root table (8-byte entries, 16-byte aligned); the
@@ -624,6 +624,7 @@ static cudaError_t rows_any(const TransformArgs& g, bool square, cudaStream_t st
         case 10: return rows_at<LazyArith, 10>(g, square, st, init);
         case 11: return rows_at<LazyArith, 11>(g, square, st, init);
         case 12: return rows_at<LazyArith, 12>(g, square, st, init);
+        case 13: return rows_at<LazyArith, 13>(g, square, st, init);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -664,7 +665,7 @@ cudaError_t init_transform_kernels() {
                     g.log_r = l;
                     g.log_c = l;
                     const bool col_ok = w ? l == 12 : l <= 11;
-                    const bool row_ok = w ? l >= 12 : l <= 12;
+                    const bool row_ok = w ? l >= 12 : l <= 13;
                     if (col_ok) e = fwd_cols_any(g, sq, sg, 0, true);
                     if (e == cudaSuccess && row_ok) e = rows_any(g, sq, 0, true);
                     if (e == cudaSuccess && col_ok) e = inv_cols_any(g, 0, true);
