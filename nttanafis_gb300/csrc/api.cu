@@ -44,6 +44,7 @@ static int g_marks_n = 0;
 static int g_marks_i = 0;
 
 void mark(cudaStream_t st) {
+    if (t_capturing) return;
     if (g_timing && g_marks_i < g_marks_n && cudaEventRecord(g_events[g_marks_i], st) == cudaSuccess) ++g_marks_i;
 }
 
@@ -553,27 +554,35 @@ static bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq
     ta.log_t = g0.log_t;
     ta.wide = g0.wide;
     const bool sign = g0.sign != 0;
+    mark(st);
     if (!g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
         note_launches(1);
-        return cuda_ok(launch_small_fused(ta, cp, sq, st), "batched fused product launch");
+        const bool ok = cuda_ok(launch_small_fused(ta, cp, sq, st), "batched fused product launch");
+        mark(st);
+        return ok;
     }
     if (g0.log_t <= kMaxBlockLog) {
         note_launches(1);
         if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return false;
+        mark(st);
     } else {
         ta.log_r = log_r;
         ta.log_c = g0.log_t - ta.log_r;
         note_launches(3);
-        if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch") ||
-            !cuda_ok(launch_rows(ta, sq, st), "batched row pass launch") ||
-            !cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch"))
-            return false;
+        if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch")) return false;
+        mark(st);
+        if (!cuda_ok(launch_rows(ta, sq, st), "batched row pass launch")) return false;
+        mark(st);
+        if (!cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch")) return false;
+        mark(st);
     }
     note_launches(1);
-    if (g0.conv)
-        return cuda_ok(launch_crt_conv_batch(descs, n, max_len, g0.log_t, cp, st), "batched CRT launch");
-    return cuda_ok(launch_crt_mul_batch(descs, n, (int)((max_len + kCrtTile - 1) / kCrtTile), g0.log_t, cp, st),
-                   "batched CRT launch");
+    const bool ok =
+        g0.conv ? cuda_ok(launch_crt_conv_batch(descs, n, max_len, g0.log_t, cp, st), "batched CRT launch")
+                : cuda_ok(launch_crt_mul_batch(descs, n, (int)((max_len + kCrtTile - 1) / kCrtTile), g0.log_t, cp, st),
+                          "batched CRT launch");
+    mark(st);
+    return ok;
 }
 
 // Enqueues a split product: the blocks of the longer operand times the shorter one

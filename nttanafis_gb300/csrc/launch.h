@@ -20,15 +20,21 @@ constexpr int kMaxLogT = 25;
 #endif
 constexpr int kCrtTile = NTT_CRT_TILE;
 
-// Column passes of the four-step: a CTA of kColThreads threads owns 2^kColLogG
-// columns; thread t takes column t mod 2^kColLogG and rows r0 + k * RS with
-// r0 = t >> kColLogG, RS = 2^kColLogRS rows per sweep, k < SW = R / RS.
+// Column passes of the four-step: a CTA of kColThreads threads owns G = 2^log_g
+// columns of R = 2^log_r points; thread t takes column t mod G and rows r0 + k * RS
+// with r0 = t / G, RS = 256 / G rows per sweep, k < SW = R / RS. G is 2^kColLogG
+// for R >= 2^9 (a row segment of G residues is one 32-byte sector) and
+// 2^(12 - log_r) below, so that the first pass, which holds 16 points of one
+// column per thread, still has a register block for every thread.
 #ifndef NTT_COLS_LOG_G
 #define NTT_COLS_LOG_G 3
 #endif
 constexpr int kColThreads = 256;
 constexpr int kColLogG = NTT_COLS_LOG_G;
-constexpr int kColLogRS = 8 - kColLogG;
+__host__ __device__ constexpr int col_group_log(int log_r) {
+    return log_r + kColLogG >= 12 ? kColLogG : 12 - log_r;
+}
+__host__ __device__ constexpr int col_log_rs(int log_r) { return 8 - col_group_log(log_r); }
 // Four-step twiddles, tabulated per prime and transform length T = R * C:
 //  - forward, applied by the column pass: w_T^(col * brev(row)). Row r0 + RS*k has
 //    the bit-reversed index brev(r0) * SW + brev(k), so the twiddle is
@@ -142,8 +148,8 @@ struct StepTableBuild {
 __host__ __device__ inline void step_table_sizes(int log_t, int log_r, u64 sizes[4]) {
     const int log_c = log_t - log_r;
     const u64 R = (u64)1 << log_r, C = (u64)1 << log_c;
-    sizes[0] = C << kColLogRS;                     // f4_a: [col][brev(r0)]
-    sizes[1] = C * (R >> kColLogRS);               // f4_b: [col][sweep]
+    sizes[0] = C << col_log_rs(log_r);             // f4_a: [col][brev(r0)]
+    sizes[1] = C * (R >> col_log_rs(log_r));       // f4_b: [col][sweep]
     sizes[2] = R << kRowTwLoBits;                  // i4_lo: [row][lo]
     sizes[3] = R * (C >> kRowTwLoBits);            // i4_hi: [row][hi]
 }

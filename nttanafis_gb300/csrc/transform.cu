@@ -45,9 +45,6 @@ __host__ __device__ constexpr int row_threads(int log_c) {
                                                 : NTT_ROW_THREADS;
 }
 
-// log2 of the columns one CTA of a column pass owns: 8 columns, so a row segment
-// is one 32-byte sector of u32 residues (two of u64 limbs).
-__host__ __device__ constexpr int col_group_log(int) { return kColLogG; }
 // Padded words per column in shared memory: congruent to 32/G mod 32 so that a
 // warp's G columns times 32/G rows fall in distinct banks.
 __host__ __device__ constexpr int col_vstride(int log_r) {
@@ -65,6 +62,7 @@ struct ColumnMap {
     static constexpr int LOG_G = col_group_log(LOG_R);
     static constexpr int G = 1 << LOG_G;
     static constexpr int VS = col_vstride(LOG_R);
+    static constexpr int LOG_RS = col_log_rs(LOG_R);
     static constexpr int RS = kThreads / G;        // rows per sweep (power of two <= 32)
     static constexpr int SWEEPS = (1 << LOG_R) / RS;
     static constexpr int LOG_SW = LOG_R - (8 - LOG_G);
@@ -110,7 +108,7 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
         for (int i = threadIdx.x; i < (M::G << M::LOG_SW); i += kThreads)
             fb[(i >> M::LOG_SW) * (M::SWEEPS + 1) + (i & (M::SWEEPS - 1))] = __ldg(src + i);
     }
-    const uint2 fa = __ldg(pp.f4_a + ((size_t)col << kColLogRS) + (__brev((u32)r0) >> (32 - kColLogRS)));
+    const uint2 fa = __ldg(pp.f4_a + ((size_t)col << M::LOG_RS) + (__brev((u32)r0) >> (32 - M::LOG_RS)));
     // First forward pass fused with the limb reduction (its roots come from global
     // memory: the shared table is published by the barrier after it). Item it takes
     // column c = it mod G and block gg = it / G (rows gg + k * HQ), so a warp loads
@@ -177,7 +175,7 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
 // (brev(row) = 32 brev5(k) + brev5(g2)). Four CTAs per SM (64 registers) measured
 // best.
 constexpr int kCol2LogR = 10;
-static_assert(kColLogG == 3 && kColLogRS == 5, "two-pass columns assume 8 columns per CTA");
+static_assert(col_group_log(10) == 3 && col_log_rs(10) == 5, "two-pass columns assume 8 columns per CTA");
 
 template <class A, bool SIGNED>
 __global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant__ TransformArgs g) {
@@ -478,14 +476,14 @@ __global__ void __launch_bounds__(256) k_step_tables(const __grid_constant__ Ste
     u64 n[4];
     step_table_sizes(b.log_t, b.log_r, n);
     const u64 mask = ((u64)1 << b.log_t) - 1;
-    const int log_sw = b.log_r - kColLogRS, log_nh = b.log_c - kRowTwLoBits;
+    const int log_rs = col_log_rs(b.log_r), log_sw = b.log_r - log_rs, log_nh = b.log_c - kRowTwLoBits;
     const u64 total = n[0] + n[1] + n[2] + n[3];
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
         u64 k = i;
         u32 x;
         uint2* out;
         if (k < n[0]) {  // w^(col * u * SW)
-            const u64 col = k >> kColLogRS, u = k & ((1u << kColLogRS) - 1);
+            const u64 col = k >> log_rs, u = k & ((1u << log_rs) - 1);
             x = power_of(b.fwd_pow, ((col * u) << log_sw) & mask, b.log_t, b.p);
             out = b.f4_a + k;
         } else if ((k -= n[0]) < n[1]) {  // w^(col * j)
@@ -528,7 +526,7 @@ cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st) {
 static size_t col_smem(int log_r, bool fwd) {
     const int log_g = col_group_log(log_r);
     const size_t words = (size_t)col_vstride(log_r) * (1 << log_g);
-    const size_t sweeps = (size_t)1 << (log_r - kColLogRS);
+    const size_t sweeps = (size_t)1 << (log_r - col_log_rs(log_r));
     return ((words * sizeof(u32) + 15) & ~(size_t)15) + ((size_t)8 << log_r) +
            (fwd ? 8 * ((size_t)1 << log_g) * (sweeps + 1) : 0);
 }
