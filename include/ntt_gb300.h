@@ -276,8 +276,9 @@ uint8_t ntt_crt_pair_combine_device(uint64_t first, uint64_t second, int64_t* d_
  * ntt_tune_splits times every split of each length in [min_log_t, max_log_t] on
  * balanced products that fill the transform (`reps` products per timing, best of
  * two) on `stream` and keeps the fastest when it beats the default by 2%; it
- * synchronizes `stream` and allocates its operands for the call. No reference
- * counterpart: the reference fixes its geometry in Geometry::select. */
+ * synchronizes `stream` and allocates its operands for the call. Calls made by other
+ * threads meanwhile may run with a split under trial (their results stay exact). No
+ * reference counterpart: the reference fixes its geometry in Geometry::select. */
 int ntt_split_set(int log_t, int log_r);
 int ntt_split_get(int log_t);
 int ntt_split_range(int log_t, int* lo, int* hi);
