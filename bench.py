@@ -487,7 +487,12 @@ def run_gpu(args) -> None:
     dev = torch.device("cuda", local)
     lib = ntt.library()
     # Four-step split per transform length, measured on this GPU (a fraction of a second).
-    splits = {} if args.no_tune else ntt.tune_splits(14, 23, reps=3, stream=torch.cuda.current_stream(dev))
+    splits = {}
+    if not args.no_tune:
+        try:
+            splits = ntt.tune_splits(14, 23, reps=3, stream=torch.cuda.current_stream(dev))
+        except RuntimeError as exc:  # e.g. no room for the tuning operands: default splits
+            print(f"split tuning skipped: {exc}", file=sys.stderr)
 
     per_step_in = 8 * (LA + LB)
     nsets = max(2, -(-2 * L2_BYTES // per_step_in))  # rotating inputs larger than L2
