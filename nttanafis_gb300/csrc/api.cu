@@ -1574,6 +1574,7 @@ uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream) {
         if (!split_range(log_t, lo, hi) || lo == hi) continue;
         // operands of 2^(log_t - 1) limbs: the product fills the transform
         const u64 n = (u64)1 << (log_t - 1);
+        const int before = g_split[log_t].load();
         float best = 1e30f, standard = 1e30f;
         int pick = log_t / 2;
         for (int r = lo; ok && r <= hi; ++r) {
@@ -1594,6 +1595,10 @@ uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream) {
                 best = ms;
                 pick = r;
             }
+        }
+        if (!ok) {  // a failed trial leaves the split as it was
+            g_split[log_t].store(before);
+            break;
         }
         // another split only when it is at least 2% faster than the default
         if (!(best < 0.98f * standard)) pick = log_t / 2;
