@@ -1133,6 +1133,7 @@ struct Composition {
     int trials = 0;     // tuning runs enqueued
     cudaEvent_t t0[kTrials] = {}, t1[kTrials] = {};
     int lanes = 0;      // chosen lane count (0: not tuned yet)
+    bool no_graph = false;  // its capture failed once: enqueued directly from then on
     cudaGraphExec_t exec = nullptr;
     uint64_t kernels = 0;  // kernel nodes, counted at every replay
 };
@@ -1311,7 +1312,11 @@ static bool capture_and_run(ntt_batch* b, Composition& e, const std::vector<Batc
                             const ProductDesc* dev_desc, cudaStream_t st, int lanes) {
     // Every table and constant the classes need exists by now (the first run built
     // them), so the capture records launches only.
-    if (!cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture")) return false;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        e.no_graph = true;
+        return enqueue_classes(b, cls, dev_desc, st, lanes);
+    }
     t_capturing = true;
     const bool recorded = enqueue_classes(b, cls, dev_desc, st, lanes);
     t_capturing = false;
@@ -1323,9 +1328,12 @@ static bool capture_and_run(ntt_batch* b, Composition& e, const std::vector<Batc
         ok = cuda_ok(cudaGraphInstantiate(&e.exec, graph, 0), "cudaGraphInstantiate");
     }
     if (graph) cudaGraphDestroy(graph);
-    if (!ok) {
+    if (!ok) {  // the capture recorded nothing that runs: enqueue directly instead
+        if (e.exec) cudaGraphExecDestroy(e.exec);
         e.exec = nullptr;
-        return false;
+        e.no_graph = true;
+        cudaGetLastError();
+        return enqueue_classes(b, cls, dev_desc, st, lanes);
     }
     if (!cuda_ok(cudaGraphLaunch(e.exec, st), "cudaGraphLaunch")) return false;
     note_launches(e.kernels);
@@ -1366,15 +1374,19 @@ static bool run_classes(ntt_batch* b, const std::vector<BatchClass>& cls, const 
     e.used = ++b->clock;
     ++e.seen;
     const int fixed = b->fixed_lanes;
-    if (!capturable) return enqueue_classes(b, cls, dev_desc, st, fixed ? fixed : (e.lanes ? e.lanes : default_lanes(cls)));
-    if (e.exec && b->graphs) {
+    const bool graphs = b->graphs && capturable && !e.no_graph;
+    if (!capturable) {
+        const int lanes = fixed ? fixed : (e.lanes ? e.lanes : default_lanes(cls));
+        return enqueue_classes(b, cls, dev_desc, st, lanes);
+    }
+    if (e.exec && graphs) {
         if (!cuda_ok(cudaGraphLaunch(e.exec, st), "cudaGraphLaunch")) return false;
         note_launches(e.kernels);
         ++b->replays;
         return true;
     }
     if (fixed) {  // the caller's lane count: no tuning, a graph from the second run
-        if (e.seen >= 2 && b->graphs) return capture_and_run(b, e, cls, dev_desc, st, fixed);
+        if (e.seen >= 2 && graphs) return capture_and_run(b, e, cls, dev_desc, st, fixed);
         return enqueue_classes(b, cls, dev_desc, st, fixed);
     }
     if (e.seen < 2) return enqueue_classes(b, cls, dev_desc, st, e.lanes ? e.lanes : default_lanes(cls));
@@ -1400,7 +1412,7 @@ static bool run_classes(ntt_batch* b, const std::vector<BatchClass>& cls, const 
         e.lanes = kLaneChoices[pick];
         ++b->tuned;
     }
-    if (!b->graphs) return enqueue_classes(b, cls, dev_desc, st, e.lanes);
+    if (!graphs) return enqueue_classes(b, cls, dev_desc, st, e.lanes);
     return capture_and_run(b, e, cls, dev_desc, st, e.lanes);
 }
 
