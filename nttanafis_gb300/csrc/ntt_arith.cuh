@@ -58,6 +58,14 @@ struct LazyArith {
     static __device__ __forceinline__ u32 mulc(u32 x, uint2 w, u32 p) {
         return shoup_mul(x, w.x, w.y, p);
     }
+    // Forward butterfly with twiddle 1: x, y in [0, 2p) -> [0, 2p), no product.
+    static __device__ __forceinline__ void dif_unit(u32& x, u32& y, u32 p) {
+        const u32 p2 = p << 1;
+        const u32 s = x + y;
+        const u32 d = x - y + p2;
+        x = sub_if_ge(s, p2);
+        y = sub_if_ge(d, p2);
+    }
     // Last forward level (twiddle 1) left open for a following product: x, y in
     // [0, 2p) -> [0, 4p), without the reductions.
     static __device__ __forceinline__ void dif_open(u32& x, u32& y, u32 p) {
@@ -119,12 +127,13 @@ struct WideArith {
         y = x - y + p;
         x = s;
     }
-    // Twiddle-1 inverse level on canonical values.
+    // Twiddle-1 butterfly on canonical values (forward and inverse alike).
     static __device__ __forceinline__ void dit_unit(u32& x, u32& y, u32 p) {
         const u32 s = x + y, d = x - y + p;
         x = sub_if_ge(s, p);
         y = sub_if_ge(d, p);
     }
+    static __device__ __forceinline__ void dif_unit(u32& x, u32& y, u32 p) { dit_unit(x, y, p); }
     static __device__ __forceinline__ void dit_unit_2p(u32& x, u32& y, u32 p) { dit_unit(x, y, p); }
     static __device__ __forceinline__ u32 pointwise(u32 a, u32 b, u32 p, u32 pni) {
         return sub_if_ge(mont_mul(a, b, p, pni), p);

@@ -18,6 +18,12 @@
 #pragma once
 #include "ntt_arith.cuh"
 
+// Butterflies whose twiddle is 1 (the first of every group when a register block
+// holds consecutive points) run without a product.
+#ifndef NTT_UNIT_C0
+#define NTT_UNIT_C0 1
+#endif
+
 // Shared-memory slot of logical index i: one pad word per 32 words.
 __host__ __device__ constexpr int pad_index(int i) { return i + (i >> 5); }
 
@@ -68,6 +74,17 @@ __device__ __forceinline__ void dif_levels(u32 (&x)[VP][1 << RB], const uint2* _
         const int half = E >> (t + 1);
 #pragma unroll
         for (int c = 0; c < half; ++c) {
+            if (NTT_UNIT_C0 && H == 1 && c == 0) {
+                // consecutive points: the first butterfly of every group has twiddle 1
+#pragma unroll
+                for (int q = 0; q < VP; ++q)
+#pragma unroll
+                    for (int b = 0; b < E; b += 2 * half) {
+                        if (HZ && t == 0) x[q][b + half] = x[q][b];
+                        else A::dif_unit(x[q][b], x[q][b + half], p);
+                    }
+                continue;
+            }
             // butterflies (m, m + half) with m = blk*2*half + c share twiddle c
             const uint2 w = twb[H * half + c * H];
 #pragma unroll
@@ -103,6 +120,13 @@ __device__ __forceinline__ void dit_levels(u32 (&x)[VP][1 << RB], const uint2* _
         }
 #pragma unroll
         for (int c = 0; c < dist; ++c) {
+            if (NTT_UNIT_C0 && H == 1 && c == 0) {  // twiddle 1: no product
+#pragma unroll
+                for (int q = 0; q < VP; ++q)
+#pragma unroll
+                    for (int b = 0; b < E; b += 2 * dist) A::dit_unit(x[q][b], x[q][b + dist], p);
+                continue;
+            }
             const uint2 w = twb[(H << t) + c * H];
 #pragma unroll
             for (int q = 0; q < VP; ++q)
