@@ -17,7 +17,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 LIBDIR = HERE / "_lib"
 LIB = LIBDIR / "libntt_gb300.so"
-SOURCES = ["api.cu", "transform.cu", "small.cu", "crt.cu", "noalloc.cu", "field.cu", "probe.cu"]
+SOURCES = ["api.cu", "plan.cu", "exec.cu", "batch.cu", "transform.cu", "small.cu", "crt.cu", "noalloc.cu",
+           "field.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
