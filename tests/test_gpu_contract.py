@@ -227,3 +227,22 @@ def test_conv_device_paths(gpu):
     torch.cuda.synchronize()
     assert np.array_equal(dst.cpu().numpy().view(np.uint64), expected)
     w.close()
+
+
+def test_butterfly_probe_and_launch_counter(gpu):
+    # the compute-ceiling probe runs (positive, plausible rate) and the launch
+    # counter grows by the kernels a product enqueues
+    rate = gpu.butterfly_rate(152, 50)
+    assert 1e11 < rate < 1e14
+    import torch
+
+    ws = gpu.GpuMulWorkspace()
+    a = torch.from_numpy(operand(5000, 1).view(np.int64)).cuda()
+    b = torch.from_numpy(operand(4000, 2).view(np.int64)).cuda()
+    dst = torch.empty(9000, dtype=torch.int64, device="cuda")
+    assert ws.mul_device(dst, a, b)
+    before = gpu.kernel_launches()
+    assert ws.mul_device(dst, a, b)
+    assert gpu.kernel_launches() - before == 4  # column, row, inverse column, CRT
+    torch.cuda.synchronize()
+    ws.close()
