@@ -23,7 +23,8 @@
  *  - a product writes exactly a_len + b_len limbs, a square 2 * a_len limbs, a
  *    convolution (a_len + b_len - 1) * stride limbs; limbs past that are preserved;
  *  - every failure returns 0 and leaves dst unmodified; success returns 1;
- *  - a == b with a_len == b_len (the same slice twice) runs the square path.
+ *  - a == b with a_len == b_len (the same slice twice) runs the square path;
+ *  - dst must not overlap a or b (the reference's &mut dst cannot alias them).
  *
  * Host-pointer calls (`*_mul`, `*_sqr`, `*_convolve`) copy the operands to the GPU,
  * run, and copy the result back before returning. Pinned (page-locked) host buffers
