@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restric
         dst = d.dst;
         flags = reinterpret_cast<u32*>(d.agg);
     }
+    wait_prior_grid();  // the residues and cleared flags of the transform before it
     // Tiles are numbered in the order CTAs start, so a tile only ever waits for
     // tiles whose CTAs are already running.
     __shared__ u32 s_tile;
@@ -294,16 +295,16 @@ template <int NP>
 static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
                        const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
     const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
-    k_crt_mul<NP><<<tiles, kCrtThreads, 0, st>>>(resid, log_t, conv_len, out_len, dst,
-                                                  reinterpret_cast<u32*>(agg), cp, nullptr);
+    launch_dependent(k_crt_mul<NP>, dim3(tiles), dim3(kCrtThreads), 0, st, resid, log_t, conv_len, out_len, dst,
+                     reinterpret_cast<u32*>(agg), cp, (const ProductDesc*)nullptr);
     if (mark) mark(st);
 }
 
 template <int NP>
 static void crt_mul_batch_np(const ProductDesc* batch, int count, int max_tiles, int log_t, const CrtParams& cp,
                              cudaStream_t st) {
-    k_crt_mul<NP><<<dim3(max_tiles, count), kCrtThreads, 0, st>>>(nullptr, log_t, 0, 0, nullptr, nullptr, cp,
-                                                                   batch);
+    launch_dependent(k_crt_mul<NP>, dim3(max_tiles, count), dim3(kCrtThreads), 0, st, (const u32*)nullptr, log_t,
+                     (u64)0, (u64)0, (u64*)nullptr, (u32*)nullptr, cp, batch);
 }
 
 cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_tiles, int log_t,

@@ -165,6 +165,36 @@ u32 lookback_timeouts();
 // Sets the message returned by ntt_last_error() on this thread.
 void set_last_error(const std::string& message);
 
+// Programmatic dependent launch between the kernels of the four-step sequence:
+// the row pass, the inverse column pass and the CRT kernel are launched so that
+// they may be scheduled while the kernel before them drains; each waits
+// (wait_prior_grid) for that kernel's completion and memory before it reads its
+// output, and each producer lets its dependent launch (release_dependents) once
+// all of its own CTAs are running. The first kernel of a product launches
+// normally, so it never overlaps the previous product. Both device calls are
+// no-ops for a kernel launched without the attribute.
+#ifndef NTT_PDL
+#define NTT_PDL 1
+#endif
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void release_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
+template <class... KArgs, class... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = NTT_PDL;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // One-time kernel attribute setup (shared-memory opt-in) for the current device.
 cudaError_t init_small_kernels();      // small.cu (called by init_transform_kernels)
 cudaError_t init_transform_kernels();

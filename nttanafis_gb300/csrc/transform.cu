@@ -81,6 +81,7 @@ template <class A, bool SIGNED, int LOG_R>
 __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     using M = ColumnMap<LOG_R>;
+    release_dependents();
     constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;  // sweeps per batch; B*RS is a multiple of 32
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
@@ -180,6 +181,7 @@ static_assert(col_group_log(10) == 3 && col_log_rs(10) == 5, "two-pass columns a
 template <class A, bool SIGNED>
 __global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
+    release_dependents();
     constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
     const int prime = blockIdx.y;
     const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z + g.op_base;
@@ -245,9 +247,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, false);
+    release_dependents();
     if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
     const int log_c = g.log_c;
     const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    wait_prior_grid();  // the row pass's output
     u32* const spec = m.spec + ((size_t)prime << g.log_t) + blockIdx.x * G + c;
     // Pass 1: levels 0-4 on rows 32 blk + k (bit-reversed spectrum in).
     {
@@ -307,6 +311,7 @@ __global__ void __launch_bounds__(row_threads(LOG_C)) k_rows(const __grid_consta
     const int row0 = blockIdx.x << LOG_RPC;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, SQUARE);
+    release_dependents();
     u32* ra = m.spec + ((size_t)prime << g.log_t) + ((size_t)row0 << LOG_C);
     const u32* rb = m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row0 << LOG_C);
     // The rows' inverse four-step factors: RPC x 64 low-digit entries, RPC x C/64 high.
@@ -318,6 +323,7 @@ __global__ void __launch_bounds__(row_threads(LOG_C)) k_rows(const __grid_consta
         for (int i = threadIdx.x; i < RPC * (NL + NH); i += kRowThreads)
             il[i] = __ldg(i < RPC * NL ? lo + i : hi + (i - RPC * NL));
     }
+    wait_prior_grid();  // the column pass's output
     // First forward pass: global -> shared. Block gg of a row holds points gg + k * HQ.
     {
         constexpr int LOG_HQ = LOG_C - RB;
@@ -411,6 +417,7 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, false);
+    release_dependents();
     if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
     const u64 step = (u64)M::RS << g.log_c;
     u32* const base = m.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
@@ -418,6 +425,7 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
     u32* s = sm + M::slot0();
     uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
     load_table<LOG_R>(tw, pp.inv);
+    wait_prior_grid();  // the row pass's output
     u32* q = base;
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {
@@ -575,8 +583,7 @@ static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st,
     if (init) return opt_in(k, NTT_ROWS_CARVEOUT);
     const dim3 grid(1u << (g.log_r - row_log_rpc(L)), g.np, g.batch ? g.count : 1);
     const size_t smem = row_smem(L, square);
-    k<<<grid, row_threads(L), smem, st>>>(g);
-    return cudaGetLastError();
+    return launch_dependent(k, grid, dim3(row_threads(L)), smem, st, g);
 }
 
 template <class A, int L>
@@ -585,13 +592,12 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
     if constexpr (L == kCol2LogR) {
         auto k = k_inv_cols2<A>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
-        k<<<grid, kThreads, col2_smem(false), st>>>(g);
+        return launch_dependent(k, grid, dim3(kThreads), col2_smem(false), st, g);
     } else {
         auto k = k_inv_cols<A, L>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
-        k<<<grid, kThreads, col_smem(L, false), st>>>(g);
+        return launch_dependent(k, grid, dim3(kThreads), col_smem(L, false), st, g);
     }
-    return cudaGetLastError();
 }
 
 static cudaError_t fwd_cols_any(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
