@@ -241,6 +241,7 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict_
                                                            const __grid_constant__ CrtParams cp,
                                                            const ProductDesc* __restrict__ batch) {
     int stride = cp.stride;
+    wait_prior_grid();  // the residues of the transform before it
     if (batch) {  // member blockIdx.y of a batch
         const ProductDesc& d = batch[blockIdx.y];
         resid = d.spec;
@@ -323,21 +324,31 @@ cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_ti
     return cudaGetLastError();
 }
 
+template <int NP>
+static cudaError_t crt_conv_np(dim3 grid, cudaStream_t st, const u32* resid, int log_t, u64 conv_len, u64* dst,
+                               const CrtParams& cp, const ProductDesc* batch) {
+    return launch_dependent(k_crt_conv<NP>, grid, dim3(kCrtThreads), 0, st, resid, log_t, conv_len, dst, cp, batch);
+}
+
+static cudaError_t crt_conv_any(dim3 grid, cudaStream_t st, const u32* resid, int log_t, u64 conv_len, u64* dst,
+                                const CrtParams& cp, const ProductDesc* batch) {
+    switch (cp.np) {
+        case 1: return crt_conv_np<1>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 2: return crt_conv_np<2>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 3: return crt_conv_np<3>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 4: return crt_conv_np<4>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 5: return crt_conv_np<5>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 6: return crt_conv_np<6>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 7: return crt_conv_np<7>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        case 8: return crt_conv_np<8>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
                                   const CrtParams& cp, cudaStream_t st) {
     const dim3 grid((unsigned)((max_conv_len + kCrtThreads - 1) / kCrtThreads), count);
-    switch (cp.np) {
-        case 1: k_crt_conv<1><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 2: k_crt_conv<2><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 3: k_crt_conv<3><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 4: k_crt_conv<4><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 5: k_crt_conv<5><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 6: k_crt_conv<6><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 7: k_crt_conv<7><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        case 8: k_crt_conv<8><<<grid, kCrtThreads, 0, st>>>(nullptr, log_t, 0, nullptr, cp, batch); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    return crt_conv_any(grid, st, nullptr, log_t, 0, nullptr, cp, batch);
 }
 
 cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
@@ -360,18 +371,7 @@ cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst,
                             const CrtParams& cp, cudaStream_t st) {
     (void)sign;  // the quotient bias in cp selects signed rounding
     const unsigned blocks = (unsigned)((conv_len + kCrtThreads - 1) / kCrtThreads);
-    switch (cp.np) {
-        case 1: k_crt_conv<1><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 2: k_crt_conv<2><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 3: k_crt_conv<3><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 4: k_crt_conv<4><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 5: k_crt_conv<5><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 6: k_crt_conv<6><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 7: k_crt_conv<7><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        case 8: k_crt_conv<8><<<blocks, kCrtThreads, 0, st>>>(resid, log_t, conv_len, dst, cp, nullptr); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    return crt_conv_any(dim3(blocks), st, resid, log_t, conv_len, dst, cp, nullptr);
 }
 
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst, int stride,
