@@ -272,7 +272,7 @@ uint8_t ntt_crt_pair_combine_device(uint64_t first, uint64_t second, int64_t* d_
  * ntt_split_set makes R = 2^log_r for transforms of 2^log_t points (0 restores the
  * default floor(log_t / 2)) and returns the previous log_r, or -1 when log_t has no
  * choice of split or log_r is outside the range that ntt_split_range reports
- * (columns 2^7..2^11, rows 2^7..2^13). ntt_split_get returns the log_r in use (0
+ * (columns 2^6..2^11, rows 2^7..2^13). ntt_split_get returns the log_r in use (0
  * for lengths without a four-step split). The split changes speed, never results.
  * ntt_tune_splits times every split of each length in [min_log_t, max_log_t] on
  * balanced products that fill the transform (`reps` products per timing, best of

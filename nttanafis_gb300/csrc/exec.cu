@@ -111,7 +111,7 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
     TransformArgs ta;
     memset(&ta, 0, sizeof(ta));
     CrtParams cp;
-    const int log_r = four_step_log_r(g);
+    const int log_r = single_log_r(g);
     if (!prepare_params(g, log_r, ta.ps, cp)) return false;
     ta.a = d_a;
     ta.b = square ? d_a : d_b;
@@ -128,7 +128,7 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
         ta.flag_words = (u32)carry_flag_words(g.out_len);
     }
     const bool sign = g.sign != 0;
-    if (!g.conv && g.log_t <= kFusedMaxLog && g.np == kFusedPrimes && !g.wide) {
+    if (!g.conv && log_r == 0 && g.log_t <= kFusedMaxLog && g.np == kFusedPrimes && !g.wide) {
         // the whole product in one cluster launch
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         ta.dst = d_dst;
@@ -138,7 +138,7 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
         mark(st);
         return ok;
     }
-    if (g.log_t <= kMaxBlockLog) {
+    if (log_r == 0) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         note_launches(1);
         if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;

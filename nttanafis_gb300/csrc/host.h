@@ -83,6 +83,10 @@ bool plan_conv(u64 la, u64 lb, u64 max_a, u64 max_b, int sign, Geom& g);
 extern std::atomic<int> g_split[kMaxLogT + 1];
 bool split_range(int log_t, int& lo, int& hi);
 int four_step_log_r(const Geom& g);
+// The split of a product or convolution enqueued alone (execute): as above, and
+// four-step with 2^6-point columns for T = 2^13, where one CTA per prime would leave
+// all but five SMs idle. Batch members of that length keep the one-CTA kernels.
+int single_log_r(const Geom& g);
 // Kernel constants of a plan with four-step split R = 2^log_r (tables built on
 // first use), or with the split in use.
 bool prepare_params(const Geom& g, int log_r, PrimeSet& ps, CrtParams& cp);

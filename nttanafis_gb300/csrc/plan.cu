@@ -320,7 +320,7 @@ static bool step_tables(int dev, u32 p, int log_t, int log_r, StepTables& out) {
     const u32 scale = mulmod(invmod((u32)(((u64)1 << log_t) % p), p), (u32)(((u64)1 << 32) % p), p);
     StepTables t;
     t.scale = shoup_pair(scale, p);
-    if (log_t > kMaxBlockLog) {
+    if (log_r > 0) {
         StepTableBuild b;
         memset(&b, 0, sizeof(b));
         b.p = p;
@@ -363,7 +363,7 @@ std::atomic<int> g_split[kMaxLogT + 1];
 // four-step form or is one of the wide lengths.
 bool split_range(int log_t, int& lo, int& hi) {
     if (log_t <= kMaxBlockLog || log_t > 23) return false;
-    lo = std::max(7, log_t - 13);
+    lo = std::max(6, log_t - 13);
     hi = std::min(11, log_t - 7);
     return lo <= hi;
 }
@@ -372,6 +372,11 @@ int four_step_log_r(const Geom& g) {
     if (g.log_t <= kMaxBlockLog) return 0;
     const int o = g.wide ? 0 : g_split[g.log_t].load(std::memory_order_relaxed);
     return o ? o : g.log_t / 2;
+}
+
+int single_log_r(const Geom& g) {
+    if (g.log_t == kMaxBlockLog && !g.wide) return 6;  // 2^6-point columns, 2^7-point rows
+    return four_step_log_r(g);
 }
 
 // Fills the kernel constants of a plan whose four-step split is R = 2^log_r (0 for

@@ -45,11 +45,13 @@ __host__ __device__ constexpr int row_threads(int log_c) {
                                                 : NTT_ROW_THREADS;
 }
 
-// Padded words per column in shared memory: congruent to 32/G mod 32 so that a
-// warp's G columns times 32/G rows fall in distinct banks.
+// Padded words per column in shared memory: congruent to 32/G mod 32 (1 when G >=
+// 32) so that a warp's G columns times 32/G rows fall in distinct banks.
+__host__ __device__ constexpr int col_words_mod(int log_r) {
+    return col_group_log(log_r) >= 5 ? 1 : 32 >> col_group_log(log_r);
+}
 __host__ __device__ constexpr int col_vstride(int log_r) {
-    return padded_len(1 << log_r) +
-           ((((32 >> col_group_log(log_r)) - padded_len(1 << log_r)) % 32) + 32) % 32;
+    return padded_len(1 << log_r) + (((col_words_mod(log_r) - padded_len(1 << log_r)) % 32) + 32) % 32;
 }
 
 // Column pass of the forward four-step: G columns of R = 2^LOG_R points per CTA.
@@ -526,7 +528,7 @@ cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------------
 // Launchers: one instantiation per transform size. The lazy arithmetic covers
-// T <= 2^23 (one-CTA sizes 2^4..2^13, columns 2^7..2^11, rows 2^7..2^13); the wide
+// T <= 2^23 (one-CTA sizes 2^4..2^13, columns 2^6..2^11, rows 2^7..2^13); the wide
 // arithmetic covers T = 2^24, 2^25 (columns 2^12, rows 2^12..2^13).
 
 // Column residues plus the level root table (8-byte entries, 16-byte aligned); the
@@ -606,6 +608,7 @@ static cudaError_t fwd_cols_any(const TransformArgs& g, bool square, bool sign, 
         return cudaErrorInvalidValue;
     }
     switch (g.log_r) {
+        case 6: return fwd_cols_at<LazyArith, 6>(g, square, sign, st, init);
         case 7: return fwd_cols_at<LazyArith, 7>(g, square, sign, st, init);
         case 8: return fwd_cols_at<LazyArith, 8>(g, square, sign, st, init);
         case 9: return fwd_cols_at<LazyArith, 9>(g, square, sign, st, init);
@@ -639,6 +642,7 @@ static cudaError_t inv_cols_any(const TransformArgs& g, cudaStream_t st, bool in
         return cudaErrorInvalidValue;
     }
     switch (g.log_r) {
+        case 6: return inv_cols_at<LazyArith, 6>(g, st, init);
         case 7: return inv_cols_at<LazyArith, 7>(g, st, init);
         case 8: return inv_cols_at<LazyArith, 8>(g, st, init);
         case 9: return inv_cols_at<LazyArith, 9>(g, st, init);
@@ -665,11 +669,11 @@ cudaError_t init_transform_kernels() {
         for (int sg = 0; sg < 2; ++sg) {
             for (int w = 0; w < 2; ++w) {
                 g.wide = w;
-                for (int l = 7; l <= 13 && e == cudaSuccess; ++l) {
+                for (int l = 6; l <= 13 && e == cudaSuccess; ++l) {
                     g.log_r = l;
                     g.log_c = l;
                     const bool col_ok = w ? l == 12 : l <= 11;
-                    const bool row_ok = w ? l >= 12 : l <= 13;
+                    const bool row_ok = w ? l >= 12 : l >= 7;
                     if (col_ok) e = fwd_cols_any(g, sq, sg, 0, true);
                     if (e == cudaSuccess && row_ok) e = rows_any(g, sq, 0, true);
                     if (e == cudaSuccess && col_ok) e = inv_cols_any(g, 0, true);

@@ -108,9 +108,9 @@ def test_block_split_choice():
 
 
 def test_split_api_ranges_and_validation():
-    # four-step splits: columns 2^7..2^11, rows 2^7..2^13, lazy lengths 2^14..2^23
+    # four-step splits: columns 2^6..2^11, rows 2^7..2^13, lazy lengths 2^14..2^23
     assert ntt.split_range(13) is None and ntt.split_range(24) is None
-    assert ntt.split_range(14) == (7, 7)
+    assert ntt.split_range(14) == (6, 7)
     assert ntt.split_range(21) == (8, 11)
     assert ntt.split_range(23) == (10, 11)
     assert ntt.get_split(21) == 10 and ntt.get_split(13) == 0
@@ -118,6 +118,8 @@ def test_split_api_ranges_and_validation():
         ntt.set_split(21, 12)
     with pytest.raises(ValueError):
         ntt.set_split(21, 7)
+    with pytest.raises(ValueError):
+        ntt.set_split(20, 6)
     with pytest.raises(ValueError):
         ntt.set_split(13, 6)
     try:

@@ -112,7 +112,7 @@ def test_fused_cluster_every_size(ws, log_t):
     assert np.array_equal(gpu_mul(ws, a, c), oracle.mul(a, c)), log_t
 
 
-@pytest.mark.parametrize("log_t", range(15, 24))
+@pytest.mark.parametrize("log_t", range(14, 24))
 def test_every_four_step_split(ws, gpu, log_t):
     # every split T = R * C the kernels offer gives the same product and square
     lo, hi = gpu.split_range(log_t)
