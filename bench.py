@@ -218,6 +218,7 @@ def configs_section(dev, stream, peak_gbs: float) -> list:
     cases = [
         ("mul 256x256", 256, 256, operand, 8000),
         ("mul 1024x1024", 1024, 1024, operand, 8000), ("sqr 1024", 1024, 0, operand, 8000),
+        ("mul 4096x4096", 4096, 4096, operand, 4000),
         ("mul 16384x16384", 1 << 14, 1 << 14, operand, 4000), ("mul 65536x65536", 1 << 16, 1 << 16, operand, 2000),
         ("mul 262144x262144", 1 << 18, 1 << 18, operand, 400),
         ("mul 1048576x1048576", 1 << 20, 1 << 20, operand, 100), ("sqr 1048576", 1 << 20, 0, operand, 100),
