@@ -165,7 +165,7 @@ static int split_log(u64 L, u64 S, int full_log) {
 
 // allow_split: callers that run one product per call (workspaces, plans) may take
 // the block split; batch members always use one transform.
-bool plan_mul(u64 la, u64 lb, Geom& g, bool allow_split) {
+static bool plan_mul_new(u64 la, u64 lb, Geom& g, bool allow_split) {
     if (!la || !lb) return fail("operand length is zero");
     const u64 L = std::max(la, lb), S = std::min(la, lb);
     const int full_log = std::max(4, ceil_log2(la + lb - 1));
@@ -204,7 +204,7 @@ static int bound_bits(u64 terms, u64 max_a, u64 max_b) {
     return bitlen128(product) + (terms > 1 ? 64 - __builtin_clzll(terms - 1) : 0);
 }
 
-bool plan_conv(u64 la, u64 lb, u64 max_a, u64 max_b, int sign, Geom& g) {
+static bool plan_conv_new(u64 la, u64 lb, u64 max_a, u64 max_b, int sign, Geom& g) {
     if (!la || !lb) return fail("operand length is zero");
     g = Geom();
     g.conv = true;
@@ -228,6 +228,39 @@ bool plan_conv(u64 la, u64 lb, u64 max_a, u64 max_b, int sign, Geom& g) {
         g.log_t = std::max(4, ceil_log2(g.conv_len));
         if (!choose_primes(g, std::max(1, g.bound_bits))) return fail("no prime set holds the coefficients");
     }
+    return true;
+}
+
+// Plans are pure functions of their arguments and batches repeat shapes, so each
+// thread keeps the admitted plans it made (failures are recomputed, to set their
+// message again). The caches are dropped whole when they grow past kPlanCache.
+constexpr size_t kPlanCache = 1 << 13;
+
+bool plan_mul(u64 la, u64 lb, Geom& g, bool allow_split) {
+    thread_local std::map<std::tuple<u64, u64, bool>, Geom> cache;
+    const auto key = std::make_tuple(la, lb, allow_split);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        g = it->second;
+        return true;
+    }
+    if (!plan_mul_new(la, lb, g, allow_split)) return false;
+    if (cache.size() >= kPlanCache) cache.clear();
+    cache.emplace(key, g);
+    return true;
+}
+
+bool plan_conv(u64 la, u64 lb, u64 max_a, u64 max_b, int sign, Geom& g) {
+    thread_local std::map<std::tuple<u64, u64, u64, u64, int>, Geom> cache;
+    const auto key = std::make_tuple(la, lb, max_a, max_b, sign);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        g = it->second;
+        return true;
+    }
+    if (!plan_conv_new(la, lb, max_a, max_b, sign, g)) return false;
+    if (cache.size() >= kPlanCache) cache.clear();
+    cache.emplace(key, g);
     return true;
 }
 
