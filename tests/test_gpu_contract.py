@@ -204,6 +204,21 @@ def test_conv_alias_and_large_shapes(gpu, cws):
                               oracle.conv(a, b, mx, mx, signed, THREADS)), (bits, signed)
 
 
+@pytest.mark.parametrize("la,lb", [(4096, 3000), (2049, 2048), (6000, 2193), (8000, 193)])
+def test_conv_single_transform_lengths_near_2_pow_13(gpu, cws, la, lb):
+    # T = 2^12 (one CTA per prime) and T = 2^13 (four-step, 2^6-point columns, when
+    # enqueued alone), at every coefficient class and sign
+    for bits, signed in [(16, False), (32, False), (31, True), (64, False)]:
+        mx = bound_of(bits)
+        if signed:
+            a, b = signed_values(operand(la, 61), mx), signed_values(operand(lb, 62), mx)
+            mx = 1 << 31
+        else:
+            a, b = operand(la, 61) & np.uint64(mx), operand(lb, 62) & np.uint64(mx)
+        assert np.array_equal(conv_gpu(gpu, cws, a, b, mx, mx, signed),
+                              oracle.conv(a, b, mx, mx, signed, THREADS)), (la, lb, bits, signed)
+
+
 def test_conv_device_paths(gpu):
     import torch
 
