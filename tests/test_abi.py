@@ -140,3 +140,19 @@ def test_split_file_round_trip(tmp_path):
         assert ntt.get_split(18) == 10
     finally:
         ntt.set_split(18, 0)
+
+
+def test_repeated_plans_are_identical_and_failures_repeat():
+    # plans are cached per thread: a repeated shape returns the same plan, and a
+    # rejected shape is rejected again with its message
+    shapes = [(1000, 900), (1 << 20, 1 << 20), (65536, 256), (2**25, 2), (7, 5)]
+    first = [ntt.MulPlan.new(a, b) for a, b in shapes]
+    again = [ntt.MulPlan.new(a, b) for a, b in shapes]
+    assert first == again
+    for _ in range(2):
+        assert ntt.MulPlan.new(2**25, 2**25) is None
+        assert ntt.last_error()
+    c1 = ntt.ConvPlan.new(3000, 2000, 0xFFFF, 0xFFFF, False)
+    c2 = ntt.ConvPlan.new(3000, 2000, 0xFFFF, 0xFFFF, False)
+    assert c1 == c2 and c1 is not None
+    assert ntt.ConvPlan.new(3000, 2000, 0xFFFF, 0xFFFF, True) != c1
