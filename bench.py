@@ -597,6 +597,17 @@ def run_gpu(args) -> None:
         run_e2e(nthreads, 2 * nthreads)
         e2e_s = run_e2e(nthreads, e2e_steps)
         e2e_one_s = run_e2e(1, e2e_steps // nthreads) / (e2e_steps // nthreads)
+        # One caller with pageable (ordinary) host buffers, what a drop-in caller
+        # passing its own slices gives the library.
+        pa, pb = host_sets[0][0].copy(), host_sets[0][1].copy()
+        pd = np.empty(LA + LB, dtype=np.uint64)
+        assert e2e_ws[0].mul(pd, pa, pb), ntt.last_error()
+        pageable_steps = max(3, min(args.steps, 20))
+        t0 = time.perf_counter()
+        for _ in range(pageable_steps):
+            if not e2e_ws[0].mul(pd, pa, pb):
+                failures.append(ntt.last_error())
+        e2e_pageable_s = (time.perf_counter() - t0) / pageable_steps
         assert not failures, failures[:1]
         e2e_ok = True
         for t in range(nthreads):
@@ -646,8 +657,15 @@ def run_gpu(args) -> None:
     # the same lazy butterfly (no memory traffic) measured now on this GPU.
     t_len = 1 << plan.log_transform
     butterflies = 3 * plan.primes * (t_len // 2) * plan.log_transform
-    probe_rate = ntt.butterfly_rate()
+    from nttanafis_gb300 import probe
+
+    probe_rate = probe.butterfly_rate()
     bfly_rate = butterflies / (ms_per_step / 1000.0)
+    # Per-butterfly cost of the candidate residue arithmetics (register-only probes):
+    # the transforms' 32-bit Shoup butterfly against a 32-bit Montgomery one, a
+    # 64-bit Shoup one over a 50-bit prime and the reference's f64 FMA one, and the
+    # raw instruction rates behind them.
+    arith = {name: probe.rate(v) for v, name in enumerate(probe.VARIANTS)}
 
     line = {
         "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
@@ -661,6 +679,7 @@ def run_gpu(args) -> None:
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": per_step_in,
                 "d2h_bytes_per_step": 8 * (LA + LB), "api": "ntt_mul_workspace_mul (host pointers, pinned)",
                 "host_threads": nthreads, "one_thread_products_per_s": 1.0 / e2e_one_s,
+                "one_thread_pageable_products_per_s": 1.0 / e2e_pageable_s,
                 "steps": e2e_steps, "parity_ok": bool(e2e_ok)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -672,6 +691,8 @@ def run_gpu(args) -> None:
                              "butterflies_per_product": butterflies,
                              "floor_ms": butterflies / probe_rate * 1000.0,
                              "peak_kind": "measured now: register-only lazy-butterfly probe (ntt_probe_butterflies)"},
+        "arith_probe": {"unit": "operations/s (butterflies for *_butterfly*, instructions otherwise)",
+                        "rates": arith},
         "kernels": kernels, "kernels_ms_total": instrumented_ms,
         "gpu_launches": launches, "wall_s": t_wall,
         "parity": {"fingerprint_ok": fingerprint_ok, "lookback_timeouts": ntt.lookback_timeouts()},

@@ -32,6 +32,16 @@
  * void*), enqueue the work and return without synchronizing; the device buffers must
  * stay valid until the stream reaches that point.
  *
+ * Failures found by the kernels themselves: every wait of the CRT carry scan is
+ * bounded, and a wait that gives up (which a working GPU never causes: it means a
+ * CTA that had started was not scheduled for about 70 ms) leaves a wrong product; a
+ * device-pointer convolution whose coefficient exceeds its bound is not written.
+ * Host-pointer calls return 0 for either. By then a page-locked dst may already
+ * hold the wrong product (the kernels write it directly when a call runs alone);
+ * other dst memory is untouched. Device-pointer calls report them afterwards in the
+ * status of their workspace or batch (ntt_*_status, NTT_STATUS_* bits); plan calls
+ * through ntt_lookback_timeouts() and ntt_conv_plan_status().
+ *
  * A workspace owns device arenas that only grow and must not be used by two threads
  * at once. Plans are plain values. The root tables are shared by all workspaces of a
  * process and built once per device.
@@ -120,13 +130,22 @@ uint8_t ntt_mul_workspace_sqr_device(ntt_mul_workspace* ws, uint64_t* d_dst, siz
  * signed bounds must lie below 2^63. */
 int ntt_conv_plan_new(uint64_t len_a, uint64_t len_b, uint64_t max_a, uint64_t max_b,
                       int is_signed, ntt_conv_plan* out);
-/* ConvPlan::convolve (src/convolve.rs:148) on device pointers with caller scratch.
- * Coefficient bounds are checked on the host copy only in the host-pointer call;
- * this call checks lengths and buffer sizes. */
+/* ConvPlan::convolve (src/convolve.rs:148) on device pointers with caller scratch
+ * (plan->scratch_len limbs; its first 512 bytes hold the admission votes, so a
+ * schoolbook plan needs them too). Lengths and buffer sizes are checked here (0,
+ * nothing enqueued); the coefficient bounds (src/convolve.rs:169-184) are checked on
+ * the GPU before anything is written: a coefficient above its bound leaves d_dst
+ * untouched, which ntt_conv_plan_status reports. */
 uint8_t ntt_conv_plan_convolve_device(const ntt_conv_plan* plan, uint64_t* d_dst,
                                       size_t dst_len, const uint64_t* d_a, size_t a_len,
                                       const uint64_t* d_b, size_t b_len, uint64_t* d_scratch,
                                       size_t scratch_len, void* stream);
+/* Outcome of the last ntt_conv_plan_convolve_device that used this scratch: waits
+ * for `stream`, then returns 1 (admitted and written), 0 (a coefficient exceeded its
+ * bound: d_dst untouched) or -1 (CUDA error or short scratch). No reference
+ * counterpart: the reference's convolve returns this as its bool. */
+int ntt_conv_plan_status(const ntt_conv_plan* plan, const uint64_t* d_scratch, size_t scratch_len,
+                         void* stream);
 
 ntt_conv_workspace* ntt_conv_workspace_new(void);
 void ntt_conv_workspace_free(ntt_conv_workspace* ws);
@@ -137,10 +156,22 @@ uint8_t ntt_conv_workspace_prepare(ntt_conv_workspace* ws, const ntt_conv_plan* 
 uint8_t ntt_conv_workspace_convolve(ntt_conv_workspace* ws, uint64_t* dst, size_t dst_len,
                                     const uint64_t* a, size_t a_len, const uint64_t* b,
                                     size_t b_len);
-/* Device-pointer form; coefficient bounds are the caller's responsibility. */
+/* Device-pointer form. Lengths and sizes are checked here; the coefficient bounds
+ * on the GPU before anything is written (a coefficient above its bound leaves d_dst
+ * untouched and sets NTT_STATUS_BOUND in ntt_conv_workspace_status). */
 uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_dst,
                                            size_t dst_len, const uint64_t* d_a, size_t a_len,
                                            const uint64_t* d_b, size_t b_len, void* stream);
+
+/* Status bits of the device-pointer calls of a workspace or batch. */
+#define NTT_STATUS_LOOKBACK 1u /* a carry look-back wait gave up: that product is wrong */
+#define NTT_STATUS_BOUND 2u    /* a convolution coefficient exceeded its bound: not written */
+/* The NTT_STATUS_* bits set by the workspace's device-pointer calls since the last
+ * query (0: every one succeeded), cleared by reading. Call it after the calls'
+ * streams have completed. No reference counterpart: the reference's calls return
+ * these failures as their bool, which an enqueued GPU call cannot. */
+uint32_t ntt_mul_workspace_status(ntt_mul_workspace* ws);
+uint32_t ntt_conv_workspace_status(ntt_conv_workspace* ws);
 
 /* One member of a batch (device pointers). kind 0: product a*b (a square when
  * a == b and a_len == b_len; empty operands write zeros); kind 1: convolution under
@@ -189,6 +220,10 @@ int ntt_batch_set_lanes(ntt_batch* batch, int lanes);
 /* out[0] runs served from a captured graph, out[1] compositions tuned, out[2]
  * lanes of the last run enqueued directly or captured, out[3] compositions held. */
 void ntt_batch_stats(const ntt_batch* batch, uint64_t* out);
+/* NTT_STATUS_* bits of the batch's runs since the last query, cleared by reading;
+ * call it after the runs' stream has completed. A convolution member with a
+ * coefficient above its bound is left unwritten (the other members complete). */
+uint32_t ntt_batch_status(ntt_batch* batch);
 
 /* Largest product (a_len + b_len - 1 coefficients) of ntt_mul_noalloc_device, and
  * the device memory its static arrays hold on every GPU that loads the library. */
@@ -220,13 +255,6 @@ uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const uint64_t* 
  * CUDA error), and switches timing off. */
 int ntt_timing_start(int count);
 int ntt_timing_stop(float* ms, int capacity);
-
-/* Compute ceiling of the transforms, for measurement tools: runs `blocks` CTAs of
- * 256 threads, each thread doing `iters` register-only radix-16 passes (32 lazy
- * butterflies per pass) with no memory traffic, and writes the milliseconds of the
- * timed launch (after one shorter warm-up launch) to *ms. Synchronizes the device.
- * No reference counterpart. */
-uint8_t ntt_probe_butterflies(int blocks, int iters, float* ms);
 
 /* ---------------------------------------------------------------------------
  * Batched modular arithmetic in 50-bit prime fields (the reference's PrimeField
@@ -289,6 +317,12 @@ uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream);
  * (each wait is bounded; a nonzero count means a result may be wrong). Synchronizes
  * the device. */
 uint32_t ntt_lookback_timeouts(void);
+/* Test hook for the failure path above: the next `count` products whose CRT uses
+ * the carry look-back start that kernel with its tile counter at 1, so no CTA
+ * takes tile 0 and the wait for it runs out (a bounded wait on a state that nothing
+ * writes; the GPU stays usable). Returns the previous count. No reference
+ * counterpart. */
+int ntt_debug_stall_lookback(int count);
 
 /* Message of the last failure on this thread ("" when none). */
 const char* ntt_last_error(void);

@@ -9,7 +9,6 @@ from .api import (  # noqa: F401
     GpuMulWorkspace,
     Request,
     MulPlan,
-    butterfly_rate,
     get_split,
     load_splits,
     save_splits,
@@ -20,6 +19,9 @@ from .api import (  # noqa: F401
     kernel_launches,
     last_error,
     lookback_timeouts,
+    debug_stall_lookback,
+    STATUS_BOUND,
+    STATUS_LOOKBACK,
     library,
 )
 from .field import CrtPair, PrimeField  # noqa: F401

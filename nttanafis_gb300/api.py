@@ -84,6 +84,10 @@ _SIGNATURES = [
     ("ntt_conv_plan_convolve_device", ctypes.c_uint8,
      [ctypes.POINTER(NttConvPlan), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_conv_plan_status", ctypes.c_int,
+     [ctypes.POINTER(NttConvPlan), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("ntt_mul_workspace_status", ctypes.c_uint32, [ctypes.c_void_p]),
+    ("ntt_conv_workspace_status", ctypes.c_uint32, [ctypes.c_void_p]),
     ("ntt_conv_workspace_new", ctypes.c_void_p, []),
     ("ntt_conv_workspace_free", None, [ctypes.c_void_p]),
     ("ntt_conv_workspace_prepare", ctypes.c_uint8, [ctypes.c_void_p, ctypes.POINTER(NttConvPlan)]),
@@ -99,17 +103,18 @@ _SIGNATURES = [
     ("ntt_batch_set_graphs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     ("ntt_batch_set_lanes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     ("ntt_batch_stats", None, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("ntt_batch_status", ctypes.c_uint32, [ctypes.c_void_p]),
     ("ntt_mul_noalloc_device", ctypes.c_uint8,
      [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p]),
     ("ntt_timing_start", ctypes.c_int, [ctypes.c_int]),
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_lookback_timeouts", ctypes.c_uint32, []),
+    ("ntt_debug_stall_lookback", ctypes.c_int, [ctypes.c_int]),
     ("ntt_split_set", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     ("ntt_split_get", ctypes.c_int, [ctypes.c_int]),
     ("ntt_split_range", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     ("ntt_tune_splits", ctypes.c_uint8, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
-    ("ntt_probe_butterflies", ctypes.c_uint8, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("ntt_field_check", ctypes.c_int, [ctypes.c_uint64]),
     ("ntt_field_mul_method", ctypes.c_int, [ctypes.c_int]),
     ("ntt_field_below", ctypes.c_uint64, [ctypes.c_uint64]),
@@ -172,6 +177,17 @@ def lookback_timeouts() -> int:
     return int(library().ntt_lookback_timeouts())
 
 
+# Status bits of device-pointer calls (NTT_STATUS_* in include/ntt_gb300.h).
+STATUS_LOOKBACK = 1  # a carry look-back wait gave up: that product is wrong
+STATUS_BOUND = 2     # a convolution coefficient exceeded its bound: not written
+
+
+def debug_stall_lookback(count: int) -> int:
+    """Test hook: the next `count` look-back CRT launches start with their tile
+    counter at 1, so the bounded wait for tile 0 runs out. Returns the previous count."""
+    return int(library().ntt_debug_stall_lookback(int(count)))
+
+
 def split_range(log_t: int) -> Optional[tuple[int, int]]:
     """(lowest, highest) log2 R of the four-step split of 2^log_t points, or None
     when that length has no choice of split."""
@@ -220,15 +236,6 @@ def load_splits(path) -> dict:
     for t, r in data.items():
         set_split(t, r)
     return data
-
-
-def butterfly_rate(blocks: int = 152 * 8, iters: int = 2000) -> float:
-    """Lazy butterflies per second of a register-only probe (no memory traffic):
-    the integer-issue ceiling of the transform kernels on this GPU."""
-    ms = ctypes.c_float(0.0)
-    if not library().ntt_probe_butterflies(blocks, iters, ctypes.byref(ms)):
-        raise RuntimeError(last_error())
-    return blocks * 256 * iters * 32 / (ms.value * 1e-3)
 
 
 def _host(arr: np.ndarray, name: str) -> np.ndarray:
@@ -348,6 +355,11 @@ class GpuMulWorkspace:
         pa, na = _dev(a)
         return bool(self._lib.ntt_mul_workspace_sqr_device(self._ws, d, nd, pa, na, _stream_handle(stream)))
 
+    def status(self) -> int:
+        """STATUS_* bits of the device-pointer calls since the last query (0: all
+        succeeded); read after their streams have completed. Reading clears them."""
+        return int(self._lib.ntt_mul_workspace_status(self._ws))
+
 
 @dataclass(frozen=True)
 class ConvPlan:
@@ -395,6 +407,13 @@ class ConvPlan:
         return bool(library().ntt_conv_plan_convolve_device(ctypes.byref(self._raw()), d, nd, pa, na, pb, nb,
                                                             ps, ns, _stream_handle(stream)))
 
+    def status(self, scratch, stream=None) -> int:
+        """Outcome of the last convolve_device that used `scratch` (waits for
+        `stream`): 1 written, 0 a coefficient exceeded its bound (dst untouched),
+        -1 error."""
+        ps, ns = _dev(scratch)
+        return int(library().ntt_conv_plan_status(ctypes.byref(self._raw()), ps, ns, _stream_handle(stream)))
+
 
 class GpuConvWorkspace:
     """Retained convolution storage (ntt_anafis ConvWorkspace, src/convolve.rs:229-281)."""
@@ -430,6 +449,11 @@ class GpuConvWorkspace:
         pb, nb = _dev(b)
         return bool(self._lib.ntt_conv_workspace_convolve_device(self._ws, d, nd, pa, na, pb, nb,
                                                                  _stream_handle(stream)))
+
+    def status(self) -> int:
+        """STATUS_* bits of the device-pointer calls since the last query (0: all
+        succeeded); read after their streams have completed. Reading clears them."""
+        return int(self._lib.ntt_conv_workspace_status(self._ws))
 
 
 class NttRequest(ctypes.Structure):
@@ -519,6 +543,11 @@ class GpuBatch:
         out = (ctypes.c_uint64 * 4)()
         self._lib.ntt_batch_stats(self._b, out)
         return {"graph_replays": out[0], "tuned": out[1], "last_lanes": out[2], "compositions": out[3]}
+
+    def status(self) -> int:
+        """STATUS_* bits of this batch's runs since the last query (0: every member
+        succeeded); read after the runs' stream has completed. Reading clears them."""
+        return int(self._lib.ntt_batch_status(self._b))
 
     @property
     def graph_replays(self) -> int:

@@ -1,8 +1,13 @@
-"""Builds the sm_103a shared library `_lib/libntt_gb300.so` in-tree with nvcc.
+"""Builds the sm_103a shared libraries in-tree with nvcc:
+
+  _lib/libntt_gb300.so  the product: the C ABI of include/ntt_gb300.h;
+  _lib/libntt_probe.so  a measurement tool (include/ntt_probe.h): register-only
+                        arithmetic probes that bench.py loads for its compute
+                        ceiling. The product never loads it.
 
 Each translation unit compiles in its own nvcc process (in parallel), then one
-link step produces the library. Only `-gencode arch=compute_103a,code=sm_103a` is
-emitted: the library targets GB300 alone.
+link step per library. Only `-gencode arch=compute_103a,code=sm_103a` is emitted:
+the libraries target GB300 alone.
 """
 from __future__ import annotations
 
@@ -17,8 +22,10 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 LIBDIR = HERE / "_lib"
 LIB = LIBDIR / "libntt_gb300.so"
+PROBE_LIB = LIBDIR / "libntt_probe.so"
 SOURCES = ["api.cu", "plan.cu", "exec.cu", "batch.cu", "transform.cu", "small.cu", "crt.cu", "noalloc.cu",
-           "field.cu", "probe.cu"]
+           "field.cu"]
+PROBE_SOURCES = ["probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,21 +40,22 @@ def nvcc() -> str:
 
 
 def _inputs() -> list[Path]:
-    files = [CSRC / s for s in SOURCES]
+    files = [CSRC / s for s in SOURCES + PROBE_SOURCES]
     files += sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h"))
-    files.append(HERE.parent / "include" / "ntt_gb300.h")
+    files += sorted((HERE.parent / "include").glob("*.h"))
     return files
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not PROBE_LIB.exists():
         return False
-    mtime = LIB.stat().st_mtime
+    mtime = min(LIB.stat().st_mtime, PROBE_LIB.stat().st_mtime)
     return all(f.stat().st_mtime <= mtime for f in _inputs())
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
-    """Compiles the library unless it is newer than every source; returns its path."""
+    """Compiles both libraries unless they are newer than every source; returns the
+    product library's path."""
     if not force and up_to_date():
         return LIB
     LIBDIR.mkdir(exist_ok=True)
@@ -71,15 +79,16 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
             raise RuntimeError(f"nvcc failed on {src}")
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as pool:
-        objs = list(pool.map(compile_one, SOURCES))
-    tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode:
-        sys.stderr.write(res.stdout + res.stderr)
-        raise RuntimeError("nvcc link failed")
-    os.replace(tmp, LIB)
+    with ThreadPoolExecutor(max_workers=len(SOURCES) + len(PROBE_SOURCES)) as pool:
+        objs = list(pool.map(compile_one, SOURCES + PROBE_SOURCES))
+    for lib, part in ((LIB, objs[:len(SOURCES)]), (PROBE_LIB, objs[len(SOURCES):])):
+        tmp = lib.with_suffix(".so.tmp")
+        cmd = [cc, "-shared", *ARCH, "-o", str(tmp), *map(str, part), "-lcudart"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode:
+            sys.stderr.write(res.stdout + res.stderr)
+            raise RuntimeError(f"nvcc link failed for {lib.name}")
+        os.replace(tmp, lib)
     return LIB
 
 

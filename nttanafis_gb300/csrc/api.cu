@@ -38,6 +38,41 @@ void mark(cudaStream_t st) {
 
 void set_last_error(const std::string& message) { g_error = message; }
 
+// Look-back CRT launches that still have to start with their tile counter at 1
+// (ntt_debug_stall_lookback).
+static std::atomic<int> g_injected_stalls{0};
+
+bool take_injected_stall() {
+    int n = g_injected_stalls.load();
+    while (n > 0 && !g_injected_stalls.compare_exchange_weak(n, n - 1)) {
+    }
+    return n > 0;
+}
+
+// Failure status bytes (launch.h) in page-locked host memory that the kernels
+// write through its device address.
+struct StatusWord {
+    u32* host = nullptr;
+    u32* dev = nullptr;
+    bool create() {
+        if (!cuda_ok(cudaHostAlloc((void**)&host, sizeof(u32), cudaHostAllocMapped), "cudaHostAlloc(status)"))
+            return false;
+        *host = 0;
+        return cuda_ok(cudaHostGetDevicePointer((void**)&dev, host, 0), "cudaHostGetDevicePointer(status)");
+    }
+    void destroy() {
+        if (host) cudaFreeHost(host);
+        host = dev = nullptr;
+    }
+    // the status bits (kStatusLookback, kStatusBound) since the last take, cleared
+    u32 take() {
+        volatile uint8_t* b = reinterpret_cast<volatile uint8_t*>(host);
+        const u32 bits = (b[0] ? kStatusLookback : 0u) | (b[1] ? kStatusBound : 0u);
+        if (bits) *reinterpret_cast<volatile u32*>(host) = 0;
+        return bits;
+    }
+};
+
 bool fail(const char* msg) {
     g_error = msg;
     return false;
@@ -63,6 +98,7 @@ struct ntt_mul_workspace {
     bool has_plan = false;
     Geom plan;
     DeviceBuf a, b, out, scratch;
+    StatusWord status;                // failures of this workspace's calls
 };
 
 struct ntt_conv_workspace {
@@ -73,6 +109,7 @@ struct ntt_conv_workspace {
     bool has_plan = false;
     Geom plan;
     DeviceBuf a, b, out, scratch;
+    StatusWord status;
 };
 
 template <class W>
@@ -83,9 +120,12 @@ static W* workspace_new() {
     ws->device = dev;
     if (!cuda_ok(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaStreamCreateWithFlags(&ws->upload, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !cuda_ok(cudaEventCreateWithFlags(&ws->b_ready, cudaEventDisableTiming), "cudaEventCreate")) {
+        !cuda_ok(cudaEventCreateWithFlags(&ws->b_ready, cudaEventDisableTiming), "cudaEventCreate") ||
+        !ws->status.create()) {
         if (ws->stream) cudaStreamDestroy(ws->stream);
         if (ws->upload) cudaStreamDestroy(ws->upload);
+        if (ws->b_ready) cudaEventDestroy(ws->b_ready);
+        ws->status.destroy();
         delete ws;
         return nullptr;
     }
@@ -104,6 +144,7 @@ static void workspace_free(W* ws) {
     cudaEventDestroy(ws->b_ready);
     cudaStreamDestroy(ws->upload);
     cudaStreamDestroy(ws->stream);
+    ws->status.destroy();
     delete ws;
 }
 
@@ -125,7 +166,9 @@ static std::atomic<int> g_host_calls{0};
 // is page-locked host memory the GPU can address and no other host-pointer call is
 // in flight, and copied out otherwise. One
 // synchronisation at the end: every check runs before the first write, and a
-// failed kernel stops the stream before the copy-out.
+// failed kernel stops the stream before the copy-out. A kernel-side failure (a
+// carry look-back wait that gave up) fails the call after the synchronisation;
+// by then the copy-out, or the direct write into page-locked dst, has happened.
 template <class W>
 static bool run_host(W* ws, const Geom& g, bool square, u64* dst, const u64* a, const u64* b) {
     const size_t out_bytes = g.out_len * sizeof(u64);
@@ -153,11 +196,16 @@ static bool run_host(W* ws, const Geom& g, bool square, u64* dst, const u64* a, 
         b_ready = ws->b_ready;
     }
     u64* out = direct ? direct : (u64*)ws->out.ptr;
-    if (!execute(g, square, (const u64*)ws->a.ptr, (const u64*)ws->b.ptr, out, ws->scratch.ptr, st, b_ready))
+    if (!execute(g, square, (const u64*)ws->a.ptr, (const u64*)ws->b.ptr, out, ws->scratch.ptr, st, b_ready,
+                 ws->status.dev))
         return false;
     if (!direct && !cuda_ok(cudaMemcpyAsync(dst, out, out_bytes, cudaMemcpyDeviceToHost, st), "copy dst"))
         return false;
-    return cuda_ok(cudaStreamSynchronize(st), "kernels");
+    if (!cuda_ok(cudaStreamSynchronize(st), "kernels")) return false;
+    const u32 bits = ws->status.take();
+    if (bits & kStatusLookback) return fail("a carry look-back wait gave up: the product is wrong");
+    if (bits & kStatusBound) return fail("a coefficient exceeds its bound");
+    return true;
 }
 
 extern "C" {
@@ -283,7 +331,7 @@ static uint8_t ws_mul_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_
     if (adm == 0)
         return cuda_ok(cudaMemsetAsync(d_dst, 0, ((size_t)a_len + b_len) * 8, st), "zero product") ? 1 : 0;
     if (!ws->scratch.ensure(g.scratch_bytes(square))) return 0;
-    return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, st) ? 1 : 0;
+    return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, st, nullptr, ws->status.dev) ? 1 : 0;
 }
 
 uint8_t ntt_mul_workspace_mul_device(ntt_mul_workspace* ws, uint64_t* d_dst, size_t dst_len, const uint64_t* d_a,
@@ -331,7 +379,24 @@ uint8_t ntt_conv_plan_convolve_device(const ntt_conv_plan* plan, uint64_t* d_dst
     if (dst_len < g.out_len) return fail("destination is shorter than the convolution");
     const bool square = d_a == d_b && a_len == b_len;
     if ((u64)scratch_len * 8 < g.scratch_bytes(square)) return fail("scratch is too short");
-    return execute(g, square, d_a, d_b, d_dst, d_scratch, (cudaStream_t)stream) ? 1 : 0;
+    return execute(g, square, d_a, d_b, d_dst, d_scratch, (cudaStream_t)stream, nullptr, nullptr, true) ? 1 : 0;
+}
+
+int ntt_conv_plan_status(const ntt_conv_plan* plan, const uint64_t* d_scratch, size_t scratch_len, void* stream) {
+    Geom g;
+    if (!conv_geom(plan, g)) return -1;
+    if (!d_scratch || (u64)scratch_len * 8 < g.head_bytes()) {
+        fail("scratch is too short");
+        return -1;
+    }
+    u32 votes[kAdmitSlots];
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!cuda_ok(cudaMemcpyAsync(votes, d_scratch, kAdmitBytes, cudaMemcpyDeviceToHost, st), "copy votes") ||
+        !cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+        return -1;
+    for (int i = 0; i < kAdmitSlots; ++i)
+        if (votes[i]) return 0;
+    return 1;
 }
 
 ntt_conv_workspace* ntt_conv_workspace_new(void) { return workspace_new<ntt_conv_workspace>(); }
@@ -380,7 +445,9 @@ uint8_t ntt_conv_workspace_convolve_device(ntt_conv_workspace* ws, uint64_t* d_d
     if (!cuda_ok(cudaSetDevice(ws->device), "cudaSetDevice")) return 0;
     const bool square = d_a == d_b && a_len == b_len;
     if (!ws->scratch.ensure(g.scratch_bytes(square))) return 0;
-    return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, (cudaStream_t)stream) ? 1 : 0;
+    return execute(g, square, d_a, d_b, d_dst, ws->scratch.ptr, (cudaStream_t)stream, nullptr, ws->status.dev, true)
+               ? 1
+               : 0;
 }
 
 int ntt_timing_start(int count) {
@@ -493,6 +560,11 @@ uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream) {
 }
 
 uint32_t ntt_lookback_timeouts(void) { return lookback_timeouts(); }
+
+uint32_t ntt_mul_workspace_status(ntt_mul_workspace* ws) { return ws ? ws->status.take() : 0; }
+uint32_t ntt_conv_workspace_status(ntt_conv_workspace* ws) { return ws ? ws->status.take() : 0; }
+
+int ntt_debug_stall_lookback(int count) { return g_injected_stalls.exchange(count < 0 ? 0 : count); }
 
 const char* ntt_last_error(void) { return g_error.c_str(); }
 uint64_t ntt_kernel_launches(void) { return g_launches.load(); }

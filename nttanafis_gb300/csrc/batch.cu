@@ -57,6 +57,9 @@ static void release_composition(Composition& c) {
 
 struct ntt_batch {
     int device = 0;
+    // failure bytes of the batch's runs (launch.h) in page-locked host memory
+    u32* status_host = nullptr;
+    u32* status_dev = nullptr;
     DeviceBuf arena;  // residues and carry flags of every member
     DeviceBuf desc;   // member descriptors
     ProductDesc* host_desc = nullptr;
@@ -82,6 +85,8 @@ static void destroy_batch_events(ntt_batch* b) {
     }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->staged) cudaEventDestroy(b->staged);
+    if (b->status_host) cudaFreeHost(b->status_host);
+    b->status_host = b->status_dev = nullptr;
     for (auto& kv : b->comps) release_composition(kv.second);
     b->comps.clear();
 }
@@ -92,7 +97,10 @@ ntt_batch* ntt_batch_new(void) {
     ntt_batch* b = new ntt_batch();
     b->device = dev;
     bool ok = cuda_ok(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate") &&
-              cuda_ok(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate");
+              cuda_ok(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate") &&
+              cuda_ok(cudaHostAlloc((void**)&b->status_host, sizeof(u32), cudaHostAllocMapped), "cudaHostAlloc") &&
+              cuda_ok(cudaHostGetDevicePointer((void**)&b->status_dev, b->status_host, 0), "cudaHostGetDevicePointer");
+    if (ok) *b->status_host = 0;
     for (int i = 0; ok && i < kBatchLanes; ++i)
         ok = cuda_ok(cudaStreamCreateWithFlags(&b->lane[i], cudaStreamNonBlocking), "cudaStreamCreate") &&
              cuda_ok(cudaEventCreateWithFlags(&b->lane_done[i], cudaEventDisableTiming), "cudaEventCreate");
@@ -128,6 +136,14 @@ int ntt_batch_set_lanes(ntt_batch* b, int lanes) {
     const int prev = b->fixed_lanes;
     if (lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4) b->fixed_lanes = lanes;
     return prev;
+}
+
+uint32_t ntt_batch_status(ntt_batch* b) {
+    if (!b || !b->status_host) return 0;
+    volatile uint8_t* v = reinterpret_cast<volatile uint8_t*>(b->status_host);
+    const u32 bits = (v[0] ? kStatusLookback : 0u) | (v[1] ? kStatusBound : 0u);
+    if (bits) *reinterpret_cast<volatile u32*>(b->status_host) = 0;
+    return bits;
 }
 
 void ntt_batch_stats(const ntt_batch* b, uint64_t* out) {
@@ -174,7 +190,8 @@ static bool enqueue_classes(ntt_batch* b, const std::vector<BatchClass>& cls, co
     b->last_lanes = lanes;
     if (lanes <= 1) {
         for (const BatchClass& c : cls)
-            if (!run_members(dev_desc + c.k, (int)(c.end - c.k), c.g, c.square, c.max_len, st)) return false;
+            if (!run_members(dev_desc + c.k, (int)(c.end - c.k), c.g, c.square, c.max_len, st, b->status_dev))
+                return false;
         return true;
     }
     if (!cuda_ok(cudaEventRecord(b->fork, st), "cudaEventRecord")) return false;
@@ -191,7 +208,9 @@ static bool enqueue_classes(ntt_batch* b, const std::vector<BatchClass>& cls, co
             if (load[l] < load[lane]) lane = l;
         load[lane] += cls[i].work;
         const BatchClass& c = cls[i];
-        if (!run_members(dev_desc + c.k, (int)(c.end - c.k), c.g, c.square, c.max_len, b->lane[lane])) return false;
+        if (!run_members(dev_desc + c.k, (int)(c.end - c.k), c.g, c.square, c.max_len, b->lane[lane],
+                         b->status_dev))
+            return false;
     }
     for (int i = 0; i < lanes; ++i)
         if (!cuda_ok(cudaEventRecord(b->lane_done[i], b->lane[i]), "cudaEventRecord") ||
@@ -390,13 +409,17 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         d.b = m.square ? r.a : r.b;
         d.la = r.a_len;
         d.lb = m.square ? r.a_len : r.b_len;
-        d.spec = (u32*)(arena + m.offset);
+        // the member's scratch: [admission votes][residues][carry flags] (host.h)
+        d.spec = (u32*)(arena + m.offset + m.g.head_bytes());
         d.conv_len = m.g.conv_len;
         d.dst = r.dst;
         d.out_len = m.g.out_len;
-        d.agg = m.g.conv ? nullptr : arena + m.offset + ((m.g.spec_words(m.square) * 4 + 255) & ~(u64)255);
+        d.agg = m.g.conv ? nullptr : (uint8_t*)d.spec + m.g.spec_bytes(m.square);
+        d.votes = m.g.conv ? (u32*)(arena + m.offset) : nullptr;
         d.square = m.square ? 1u : 0u;
         d.stride = (u32)m.g.stride;
+        d.max_a = m.g.max_a;
+        d.max_b = m.square ? m.g.max_a : m.g.max_b;
     }
     if (!cuda_ok(cudaMemcpyAsync(b->desc.ptr, b->host_desc, members.size() * sizeof(ProductDesc),
                                  cudaMemcpyHostToDevice, st),
@@ -421,8 +444,12 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         if (g0.conv && g0.schoolbook) {
             for (size_t i = k; i < end; ++i) {
                 const ProductDesc& d = b->host_desc[i];
-                note_launches(1);
-                if (!cuda_ok(launch_conv_schoolbook(d.a, d.la, d.b, d.lb, d.dst, (int)d.stride, g0.sign != 0, st),
+                note_launches(2);
+                u32* votes = d.votes;
+                if (!cuda_ok(launch_conv_admit(d.a, d.la, d.b, d.lb, d.max_a, d.max_b, g0.sign != 0, votes, st),
+                             "admission launch") ||
+                    !cuda_ok(launch_conv_schoolbook(d.a, d.la, d.b, d.lb, d.dst, (int)d.stride, g0.sign != 0, st,
+                                                    votes, b->status_dev),
                              "conv schoolbook launch"))
                     return 0;
             }

@@ -18,6 +18,7 @@
 // and the descriptors of its blocks (k_split_descs).
 #include "crt.cuh"
 #include "launch.h"
+#include "transform_common.cuh"
 
 namespace ntt {
 
@@ -75,26 +76,29 @@ __device__ __forceinline__ bool look_back(volatile u32* status, u32 t, u32& cin)
 // Carries of a tile of kCrtTile limbs held four per thread, each limb with its
 // (generate, propagate) bits: the thread's composite, an inclusive warp scan, the
 // warps in order, and the tiles before this one by the decoupled look-back
-// (flags: [0] tile counter, [1] error word, [2 + t] state of tile t). Returns the
-// carry into the thread's first limb. Every thread of the CTA calls it (two
-// barriers).
+// (flags: [0] tile counter, [1] error word, [2 + t] state of tile t). A wait that
+// gives up is reported in the status bytes (launch.h) as well. Returns the carry
+// into the thread's first limb. Every thread of the CTA calls it (two barriers).
 __device__ __forceinline__ u32 tile_carry_in(const u32 (&gb)[kCrtPer], const u32 (&pb)[kCrtPer], u32 tile,
-                                             u32* flags) {
+                                             u32* flags, u32* status) {
     __shared__ u32 s_cin;
     u32 xg, xp, tg, tp;
     tile_scan(gb, pb, xg, xp, tg, tp);
     if (threadIdx.x == 0) {
-        u32* status = flags + 2;
+        u32* state = flags + 2;
         u32 cin = 0;
         if (tile > 0) {
-            atomicExch(status + tile, kTileAggregate | (tg << 2) | (tp << 3));
-            if (!look_back(status, tile, cin)) {
+            atomicExch(state + tile, kTileAggregate | (tg << 2) | (tp << 3));
+            if (!look_back(state, tile, cin)) {
+                // the product is wrong: counted, flagged in the call's error word
+                // and in the caller's status, which fails the call
                 atomicAdd(&g_lookback_timeouts, 1u);
                 atomicOr(&flags[1], 1u);
+                report_status(status, 0);
                 cin = 0;
             }
         }
-        atomicExch(status + tile, kTileInclusive | ((tg | (tp & cin)) << 2));
+        atomicExch(state + tile, kTileInclusive | ((tg | (tp & cin)) << 2));
         s_cin = cin;
     }
     __syncthreads();
@@ -117,7 +121,8 @@ __global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restric
                                                           u64 conv_len, u64 out_len, u64* __restrict__ dst,
                                                           u32* __restrict__ flags,
                                                           const __grid_constant__ CrtParams cp,
-                                                          const ProductDesc* __restrict__ batch) {
+                                                          const ProductDesc* __restrict__ batch,
+                                                          u32* __restrict__ status) {
     constexpr int L = crt_limb_words(NP);
     if (batch) {  // member blockIdx.y of a batch: grid.x covers its largest member
         const ProductDesc& d = batch[blockIdx.y];
@@ -182,13 +187,14 @@ __global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restric
     u64 sv[kCrtPer];
     u32 gb[kCrtPer], pb[kCrtPer];
     tile_limbs<L>(cw, s_pre, sv, gb, pb);
-    store_limbs(dst, k0, out_len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags));
+    store_limbs(dst, k0, out_len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags, status));
 }
 
 // dst[j] += add[j] for j < len as one big-integer addition (the sum fits in len
 // limbs): four limbs per thread, carries resolved like those of k_crt_mul.
 __global__ void __launch_bounds__(kCrtThreads) k_add_limbs(u64* __restrict__ dst, const u64* __restrict__ add,
-                                                            u64 len, u32* __restrict__ flags) {
+                                                            u64 len, u32* __restrict__ flags,
+                                                            u32* __restrict__ status) {
     __shared__ u32 s_tile;
     if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
     __syncthreads();
@@ -205,7 +211,7 @@ __global__ void __launch_bounds__(kCrtThreads) k_add_limbs(u64* __restrict__ dst
         gb[i] = t < d ? 1u : 0u;
         pb[i] = t == ~0ull ? 1u : 0u;
     }
-    store_limbs(dst, k0, len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags));
+    store_limbs(dst, k0, len, sv, gb, pb, tile_carry_in(gb, pb, tile, flags, status));
 }
 
 // Descriptors of blocks first .. first + count - 1 of a split product: block m
@@ -231,15 +237,75 @@ __global__ void k_split_descs(ProductDesc* __restrict__ d, u64 first, u64 count,
     x.agg = base + spec_bytes;
     x.square = 0;
     x.stride = 1;
+    x.max_a = x.max_b = 0;
+    x.votes = nullptr;
     d[i] = x;
 }
 
-// Disjoint blocks: coefficient k fills limbs [k*stride, (k+1)*stride).
+// Whether a convolution may be written: false when any admission vote is set
+// (votes: kAdmitSlots words, or null when the coefficients were admitted on the
+// host). Every thread of the CTA calls it (one barrier).
+__device__ __forceinline__ bool admitted(const u32* __restrict__ votes) {
+    if (!votes) return true;
+    int bad = 0;
+    for (int i = threadIdx.x; i < kAdmitSlots; i += blockDim.x) bad |= __ldcg(votes + i) != 0u;
+    return !__syncthreads_or(bad);
+}
+
+// Admission scan (src/convolve.rs:169-184) for the convolutions whose transform
+// does not load every coefficient in one CTA: CTA s of a convolution reads every
+// (kAdmitSlots)-th stretch of a and b, compares each coefficient with its bound
+// (the magnitude of a two's complement coefficient when signed) and writes vote s.
+// Each thread keeps kAdmitUnroll loads in flight, so that the scan runs near the
+// HBM rate. grid = (kAdmitSlots, members); a single convolution passes its
+// arguments, a batch class its descriptors.
+constexpr int kAdmitThreads = 1024, kAdmitUnroll = 8;
+
+template <bool SIGNED>
+__device__ __forceinline__ int scan_over(const u64* __restrict__ v, u64 n, u64 mx) {
+    int bad = 0;
+    const u64 stride = (u64)kAdmitSlots * kAdmitThreads;
+    u64 i = (u64)blockIdx.x * kAdmitThreads + threadIdx.x;
+    for (; i + (kAdmitUnroll - 1) * stride < n; i += kAdmitUnroll * stride) {
+        u64 x[kAdmitUnroll];
+#pragma unroll
+        for (int u = 0; u < kAdmitUnroll; ++u) x[u] = __ldcs(v + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < kAdmitUnroll; ++u) bad |= coefficient_over<SIGNED>(x[u], mx);
+    }
+    for (; i < n; i += stride) bad |= coefficient_over<SIGNED>(__ldcs(v + i), mx);
+    return bad;
+}
+
+template <bool SIGNED>
+__global__ void __launch_bounds__(kAdmitThreads) k_conv_admit(const u64* __restrict__ a, u64 la,
+                                                              const u64* __restrict__ b, u64 lb, u64 max_a,
+                                                              u64 max_b, u32* __restrict__ votes,
+                                                              const ProductDesc* __restrict__ batch) {
+    if (batch) {
+        const ProductDesc& d = batch[blockIdx.y];
+        a = d.a;
+        b = d.b;
+        la = d.la;
+        lb = d.lb;
+        max_a = d.max_a;
+        max_b = d.max_b;
+        votes = d.votes;
+    }
+    int bad = scan_over<SIGNED>(a, la, max_a);
+    if (b != a || lb != la || max_b != max_a) bad |= scan_over<SIGNED>(b, lb, max_b);
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) votes[blockIdx.x] = bad ? 1u : 0u;
+}
+
+// A convolution whose admission votes (launch.h) reject it is left unwritten and
+// reported in the status bytes.
 template <int NP>
 __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict__ resid, int log_t,
                                                            u64 conv_len, u64* __restrict__ dst,
                                                            const __grid_constant__ CrtParams cp,
-                                                           const ProductDesc* __restrict__ batch) {
+                                                           const ProductDesc* __restrict__ batch,
+                                                           const u32* __restrict__ votes, u32* __restrict__ status) {
     int stride = cp.stride;
     wait_prior_grid();  // the residues of the transform before it
     if (batch) {  // member blockIdx.y of a batch
@@ -248,6 +314,12 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict_
         conv_len = d.conv_len;
         dst = d.dst;
         stride = (int)d.stride;
+        votes = d.votes;
+    }
+    if ((u64)blockIdx.x * blockDim.x >= conv_len) return;
+    if (!admitted(votes)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) report_status(status, 1);
+        return;
     }
     const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= conv_len) return;
@@ -266,7 +338,13 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict_
 template <bool SIGNED>
 __global__ void __launch_bounds__(kCrtThreads) k_conv_school(const u64* __restrict__ a, u64 la,
                                                               const u64* __restrict__ b, u64 lb,
-                                                              u64* __restrict__ dst, int stride) {
+                                                              u64* __restrict__ dst, int stride,
+                                                              const u32* __restrict__ votes,
+                                                              u32* __restrict__ status) {
+    if (!admitted(votes)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) report_status(status, 1);
+        return;
+    }
     const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
     if (k + 1 >= la + lb) return;
     const u64 i_lo = k + 1 > lb ? k + 1 - lb : 0;
@@ -292,100 +370,93 @@ __global__ void __launch_bounds__(kCrtThreads) k_conv_school(const u64* __restri
 
 // ---------------------------------------------------------------------------------
 
-template <int NP>
-static void crt_mul_np(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
-                       const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
-    const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
-    launch_dependent(k_crt_mul<NP>, dim3(tiles), dim3(kCrtThreads), 0, st, resid, log_t, conv_len, out_len, dst,
-                     reinterpret_cast<u32*>(agg), cp, (const ProductDesc*)nullptr);
-    if (mark) mark(st);
-}
-
-template <int NP>
-static void crt_mul_batch_np(const ProductDesc* batch, int count, int max_tiles, int log_t, const CrtParams& cp,
-                             cudaStream_t st) {
-    launch_dependent(k_crt_mul<NP>, dim3(max_tiles, count), dim3(kCrtThreads), 0, st, (const u32*)nullptr, log_t,
-                     (u64)0, (u64)0, (u64*)nullptr, (u32*)nullptr, cp, batch);
+// Launches k_crt_mul<NP> for NP = cp.np (1..8).
+template <class... Args>
+static cudaError_t crt_mul_any(int np, dim3 grid, cudaStream_t st, Args... args) {
+    switch (np) {
+        case 1: return launch_dependent(k_crt_mul<1>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 2: return launch_dependent(k_crt_mul<2>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 3: return launch_dependent(k_crt_mul<3>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 4: return launch_dependent(k_crt_mul<4>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 5: return launch_dependent(k_crt_mul<5>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 6: return launch_dependent(k_crt_mul<6>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 7: return launch_dependent(k_crt_mul<7>, grid, dim3(kCrtThreads), 0, st, args...);
+        case 8: return launch_dependent(k_crt_mul<8>, grid, dim3(kCrtThreads), 0, st, args...);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_tiles, int log_t,
-                                 const CrtParams& cp, cudaStream_t st) {
-    switch (cp.np) {
-        case 1: crt_mul_batch_np<1>(batch, count, max_tiles, log_t, cp, st); break;
-        case 2: crt_mul_batch_np<2>(batch, count, max_tiles, log_t, cp, st); break;
-        case 3: crt_mul_batch_np<3>(batch, count, max_tiles, log_t, cp, st); break;
-        case 4: crt_mul_batch_np<4>(batch, count, max_tiles, log_t, cp, st); break;
-        case 5: crt_mul_batch_np<5>(batch, count, max_tiles, log_t, cp, st); break;
-        case 6: crt_mul_batch_np<6>(batch, count, max_tiles, log_t, cp, st); break;
-        case 7: crt_mul_batch_np<7>(batch, count, max_tiles, log_t, cp, st); break;
-        case 8: crt_mul_batch_np<8>(batch, count, max_tiles, log_t, cp, st); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+                                 const CrtParams& cp, cudaStream_t st, u32* status) {
+    return crt_mul_any(cp.np, dim3(max_tiles, count), st, (const u32*)nullptr, log_t, (u64)0, (u64)0,
+                       (u64*)nullptr, (u32*)nullptr, cp, batch, status);
 }
 
-template <int NP>
-static cudaError_t crt_conv_np(dim3 grid, cudaStream_t st, const u32* resid, int log_t, u64 conv_len, u64* dst,
-                               const CrtParams& cp, const ProductDesc* batch) {
-    return launch_dependent(k_crt_conv<NP>, grid, dim3(kCrtThreads), 0, st, resid, log_t, conv_len, dst, cp, batch);
+cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
+                           const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t), u32* status) {
+    const int tiles = (int)((out_len + kCrtTile - 1) / kCrtTile);
+    const cudaError_t e = crt_mul_any(cp.np, dim3(tiles), st, resid, log_t, conv_len, out_len, dst,
+                                      reinterpret_cast<u32*>(agg), cp, (const ProductDesc*)nullptr, status);
+    if (mark) mark(st);
+    return e;
 }
 
+// Launches k_crt_conv<NP> for NP = cp.np (1..8).
 static cudaError_t crt_conv_any(dim3 grid, cudaStream_t st, const u32* resid, int log_t, u64 conv_len, u64* dst,
-                                const CrtParams& cp, const ProductDesc* batch) {
+                                const CrtParams& cp, const ProductDesc* batch, const u32* votes, u32* status) {
     switch (cp.np) {
-        case 1: return crt_conv_np<1>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 2: return crt_conv_np<2>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 3: return crt_conv_np<3>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 4: return crt_conv_np<4>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 5: return crt_conv_np<5>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 6: return crt_conv_np<6>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 7: return crt_conv_np<7>(grid, st, resid, log_t, conv_len, dst, cp, batch);
-        case 8: return crt_conv_np<8>(grid, st, resid, log_t, conv_len, dst, cp, batch);
+#define NTT_CRT_CONV(NP)                                                                                     \
+    case NP:                                                                                                 \
+        return launch_dependent(k_crt_conv<NP>, grid, dim3(kCrtThreads), 0, st, resid, log_t, conv_len, dst, \
+                                cp, batch, votes, status);
+        NTT_CRT_CONV(1) NTT_CRT_CONV(2) NTT_CRT_CONV(3) NTT_CRT_CONV(4)
+        NTT_CRT_CONV(5) NTT_CRT_CONV(6) NTT_CRT_CONV(7) NTT_CRT_CONV(8)
+#undef NTT_CRT_CONV
         default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
-                                  const CrtParams& cp, cudaStream_t st) {
+                                  const CrtParams& cp, cudaStream_t st, u32* status) {
     const dim3 grid((unsigned)((max_conv_len + kCrtThreads - 1) / kCrtThreads), count);
-    return crt_conv_any(grid, st, nullptr, log_t, 0, nullptr, cp, batch);
-}
-
-cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst, uint8_t* agg,
-                           const CrtParams& cp, cudaStream_t st, void (*mark)(cudaStream_t)) {
-    switch (cp.np) {
-        case 1: crt_mul_np<1>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 2: crt_mul_np<2>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 3: crt_mul_np<3>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 4: crt_mul_np<4>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 5: crt_mul_np<5>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 6: crt_mul_np<6>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 7: crt_mul_np<7>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        case 8: crt_mul_np<8>(resid, log_t, conv_len, out_len, dst, agg, cp, st, mark); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    return crt_conv_any(grid, st, nullptr, log_t, 0, nullptr, cp, batch, nullptr, status);
 }
 
 cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst, bool sign,
-                            const CrtParams& cp, cudaStream_t st) {
+                            const CrtParams& cp, cudaStream_t st, const u32* votes, u32* status) {
     (void)sign;  // the quotient bias in cp selects signed rounding
     const unsigned blocks = (unsigned)((conv_len + kCrtThreads - 1) / kCrtThreads);
-    return crt_conv_any(dim3(blocks), st, resid, log_t, conv_len, dst, cp, nullptr);
+    return crt_conv_any(dim3(blocks), st, resid, log_t, conv_len, dst, cp, nullptr, votes, status);
 }
 
-cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst, int stride,
-                                   bool sign, cudaStream_t st) {
-    const u64 n = la + lb - 1;
-    const unsigned blocks = (unsigned)((n + kCrtThreads - 1) / kCrtThreads);
-    if (sign) k_conv_school<true><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride);
-    else k_conv_school<false><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride);
+cudaError_t launch_conv_admit(const u64* a, u64 la, const u64* b, u64 lb, u64 max_a, u64 max_b, bool sign,
+                              u32* votes, cudaStream_t st) {
+    if (sign)
+        k_conv_admit<true><<<kAdmitSlots, kAdmitThreads, 0, st>>>(a, la, b, lb, max_a, max_b, votes, nullptr);
+    else
+        k_conv_admit<false><<<kAdmitSlots, kAdmitThreads, 0, st>>>(a, la, b, lb, max_a, max_b, votes, nullptr);
     return cudaGetLastError();
 }
 
-cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st) {
+cudaError_t launch_conv_admit_batch(const ProductDesc* batch, int count, bool sign, cudaStream_t st) {
+    const dim3 grid(kAdmitSlots, count);
+    if (sign) k_conv_admit<true><<<grid, kAdmitThreads, 0, st>>>(nullptr, 0, nullptr, 0, 0, 0, nullptr, batch);
+    else k_conv_admit<false><<<grid, kAdmitThreads, 0, st>>>(nullptr, 0, nullptr, 0, 0, 0, nullptr, batch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst, int stride,
+                                   bool sign, cudaStream_t st, const u32* votes, u32* status) {
+    const u64 n = la + lb - 1;
+    const unsigned blocks = (unsigned)((n + kCrtThreads - 1) / kCrtThreads);
+    if (sign) k_conv_school<true><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride, votes, status);
+    else k_conv_school<false><<<blocks, kCrtThreads, 0, st>>>(a, la, b, lb, dst, stride, votes, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st, u32* status) {
     const u64 tiles = (len + kCrtTile - 1) / kCrtTile;
-    k_add_limbs<<<(unsigned)tiles, kCrtThreads, 0, st>>>(dst, add, len, flags);
+    k_add_limbs<<<(unsigned)tiles, kCrtThreads, 0, st>>>(dst, add, len, flags, status);
     return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 // residues, the limb sums of a tile held four limbs per thread, and the carry scan
 // inside a tile. See crt.cu for the algorithm and its reference.
 #pragma once
+#include "crt_chains.cuh"
 #include "launch.h"
 
 namespace ntt {
@@ -23,41 +24,21 @@ __device__ __forceinline__ void crt_words(const u32 (&r)[NP], const CrtParams& c
         y[i] = v;
         f = fmaf((float)v, cp.pinv[i], f);
     }
-    constexpr int MW = NP > 1 ? NP - 1 : 1;  // words of P/p_i
     // S = sum_i y_i * M_i in NP + 1 words (the top word stays zero), by carry
     // chains: the low halves of y_i * M_i[w] into word w, the high halves into w+1.
     u32 S[NP + 1];
 #pragma unroll
     for (int w = 0; w <= NP; ++w) S[w] = 0;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const u32 yi = y[i];
-        asm volatile("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(S[0]) : "r"(yi), "r"(cp.M[i][0]));
-#pragma unroll
-        for (int w = 1; w < MW; ++w)
-            asm volatile("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(S[w]) : "r"(yi), "r"(cp.M[i][w]));
-#pragma unroll
-        for (int w = MW; w <= NP; ++w) asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(S[w]));
-        asm volatile("mad.hi.cc.u32 %0, %1, %2, %0;" : "+r"(S[1]) : "r"(yi), "r"(cp.M[i][0]));
-#pragma unroll
-        for (int w = 2; w <= MW; ++w)
-            asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(S[w]) : "r"(yi), "r"(cp.M[i][w - 1]));
-#pragma unroll
-        for (int w = MW + 1; w <= NP; ++w) asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(S[w]));
-    }
+    for (int i = 0; i < NP; ++i) CrtChains<NP>::accumulate(S, y[i], cp.M[i]);
     // X = S - q*P in NP + 1 words; the top word is the sign (0 or all ones).
     const u32 q = (u32)(f + cp.bias);
     u32 U[NP + 1];
 #pragma unroll
     for (int w = 0; w < NP; ++w) U[w] = q * cp.P[w];
     U[NP] = 0;
-    asm volatile("mad.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[1]) : "r"(q), "r"(cp.P[0]));
-#pragma unroll
-    for (int w = 2; w <= NP; ++w)
-        asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(U[w]) : "r"(q), "r"(cp.P[w - 1]));
-    asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(x[0]) : "r"(S[0]), "r"(U[0]));
-#pragma unroll
-    for (int w = 1; w <= NP; ++w) asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(x[w]) : "r"(S[w]), "r"(U[w]));
+    CrtChains<NP>::high_products(U, q, cp.P);
+    CrtChains<NP>::subtract(x, S, U);
 }
 
 // The first W u64 words of X (sign-filled above its NP + 1 u32 words).

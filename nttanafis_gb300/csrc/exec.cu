@@ -13,7 +13,8 @@ namespace ntt {
 // Enqueues the kernels of `n` members of one transform class (same kind, length,
 // primes, sign and square) whose descriptors sit in device memory; max_len is the
 // longest member output (limbs of a product, coefficients of a convolution).
-bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st) {
+bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st,
+                 u32* status) {
     TransformArgs ta;
     memset(&ta, 0, sizeof(ta));
     CrtParams cp;
@@ -26,6 +27,14 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
     ta.wide = g0.wide;
     const bool sign = g0.sign != 0;
     mark(st);
+    // coefficient bounds of every convolution member (its votes): checked by the
+    // one-CTA transform as it loads them, or else by a scan kernel first
+    ta.admit = g0.conv ? 1 : 0;
+    if (g0.conv && g0.log_t > kMaxBlockLog) {
+        note_launches(1);
+        if (!cuda_ok(launch_conv_admit_batch(descs, n, sign, st), "batched admission launch")) return false;
+        mark(st);
+    }
     if (!g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
         note_launches(1);
         const bool ok = cuda_ok(launch_small_fused(ta, cp, sq, st), "batched fused product launch");
@@ -49,8 +58,9 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
     }
     note_launches(1);
     const bool ok =
-        g0.conv ? cuda_ok(launch_crt_conv_batch(descs, n, max_len, g0.log_t, cp, st), "batched CRT launch")
-                : cuda_ok(launch_crt_mul_batch(descs, n, (int)((max_len + kCrtTile - 1) / kCrtTile), g0.log_t, cp, st),
+        g0.conv ? cuda_ok(launch_crt_conv_batch(descs, n, max_len, g0.log_t, cp, st, status), "batched CRT launch")
+                : cuda_ok(launch_crt_mul_batch(descs, n, (int)((max_len + kCrtTile - 1) / kCrtTile), g0.log_t, cp, st,
+                                               status),
                           "batched CRT launch");
     mark(st);
     return ok;
@@ -59,7 +69,8 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
 // Enqueues a split product: the blocks of the longer operand times the shorter one
 // as batch members in chunks (the even blocks' products straight into dst, the odd
 // ones' into a second number), then dst += odd with carries.
-static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_dst, void* scratch, cudaStream_t st) {
+static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_dst, void* scratch, cudaStream_t st,
+                          u32* status) {
     const bool swap = g.la < g.lb;
     const u64* lng = swap ? d_b : d_a;
     const u64* sht = swap ? d_a : d_b;
@@ -69,7 +80,7 @@ static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_
     u64* odd = (u64*)(base + g.split_desc_bytes());
     u32* flags = (u32*)((uint8_t*)odd + g.split_odd_bytes());
     uint8_t* arena = (uint8_t*)flags + g.split_flag_bytes();
-    const u64 member = g.member_bytes(false), spec = (g.spec_words(false) * 4 + 255) & ~(u64)255;
+    const u64 member = g.member_bytes(false), spec = g.spec_bytes(false);
     if (!cuda_ok(cudaMemsetAsync(d_dst, 0, g.out_len * 8, st), "zero product") ||
         !cuda_ok(cudaMemsetAsync(odd, 0, g.out_len * 8, st), "zero odd blocks") ||
         !cuda_ok(cudaMemsetAsync(flags, 0, carry_scratch_bytes(g.out_len), st), "zero carry flags"))
@@ -81,29 +92,44 @@ static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_
         if (!cuda_ok(launch_split_descs(descs, first, count, lng, L, sht, S, g.block, d_dst, odd, arena, member, spec,
                                         st),
                      "split descriptors") ||
-            !run_members(descs, (int)count, g, false, g.block + S, st))
+            !run_members(descs, (int)count, g, false, g.block + S, st, status))
             return false;
     }
     note_launches(1);
-    return cuda_ok(launch_add_limbs(d_dst, odd, g.out_len, flags, st), "block sum");
+    return cuda_ok(launch_add_limbs(d_dst, odd, g.out_len, flags, st, status), "block sum");
 }
 
 // Enqueues one product or convolution on `st`. With `b_ready` set (an event that
 // completes when operand b is in place), the column pass of a runs first and the
 // one of b waits for that event, so b's upload overlaps a's pass.
 bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst,
-                    void* scratch, cudaStream_t st, cudaEvent_t b_ready) {
+             void* scratch, cudaStream_t st, cudaEvent_t b_ready, u32* status, bool admit) {
     mark(st);
     if (g.split()) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
-        const bool ok = execute_split(g, d_a, square ? d_a : d_b, d_dst, scratch, st);
+        const bool ok = execute_split(g, d_a, square ? d_a : d_b, d_dst, scratch, st, status);
         mark(st);
         return ok;
     }
+    // Device-side admission of a convolution's coefficients: votes at the start of
+    // the scratch, written by the one-CTA transform as it loads the coefficients,
+    // or else by a scan kernel first.
+    u32* votes = g.conv && admit ? (u32*)scratch : nullptr;
+    if (votes && (g.schoolbook || single_log_r(g) != 0)) {
+        if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
+        b_ready = nullptr;
+        note_launches(1);
+        if (!cuda_ok(launch_conv_admit(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, g.max_a,
+                                       square ? g.max_a : g.max_b, g.sign != 0, votes, st),
+                     "admission launch"))
+            return false;
+        mark(st);
+    }
     if (g.conv && g.schoolbook) {
+        if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         note_launches(1);
         const bool ok = cuda_ok(launch_conv_schoolbook(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst,
-                                                       (int)g.stride, g.sign != 0, st),
+                                                       (int)g.stride, g.sign != 0, st, votes, status),
                                 "conv schoolbook launch");
         mark(st);
         return ok;
@@ -117,14 +143,14 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
     ta.b = square ? d_a : d_b;
     ta.la = g.la;
     ta.lb = square ? g.la : g.lb;
-    ta.spec = (u32*)scratch;
+    ta.spec = (u32*)((uint8_t*)scratch + g.head_bytes());
     ta.conv_len = g.conv_len;
     ta.np = g.np;
     ta.log_t = g.log_t;
     ta.wide = g.wide;
-    const u64 spec_bytes = (g.spec_words(square) * 4 + 255) & ~(u64)255;
+    const u64 spec_bytes = g.spec_bytes(square);
     if (!g.conv) {
-        ta.flags = (u32*)((uint8_t*)scratch + spec_bytes);
+        ta.flags = (u32*)((uint8_t*)ta.spec + spec_bytes);
         ta.flag_words = (u32)carry_flag_words(g.out_len);
     }
     const bool sign = g.sign != 0;
@@ -140,6 +166,9 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
     }
     if (log_r == 0) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
+        ta.votes = votes;
+        ta.max_a = g.max_a;
+        ta.max_b = square ? g.max_a : g.max_b;
         note_launches(1);
         if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
         mark(st);
@@ -167,13 +196,17 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
     }
     if (g.conv) {
         note_launches(1);
-        const bool ok = cuda_ok(launch_crt_conv(ta.spec, g.log_t, g.conv_len, d_dst, sign, cp, st), "CRT launch");
+        const bool ok =
+            cuda_ok(launch_crt_conv(ta.spec, g.log_t, g.conv_len, d_dst, sign, cp, st, votes, status), "CRT launch");
         mark(st);
         return ok;
     }
+    if (take_injected_stall() &&
+        !cuda_ok(cudaMemsetAsync(ta.flags, 1, 1, st), "stall injection"))  // tile counter = 1
+        return false;
     note_launches(1);
-    return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst,
-                                  (uint8_t*)scratch + spec_bytes, cp, st, mark),
+    return cuda_ok(launch_crt_mul(ta.spec, g.log_t, g.conv_len, g.out_len, d_dst, (uint8_t*)ta.flags, cp, st,
+                                  mark, status),
                    "CRT launch");
 }
 

@@ -51,12 +51,18 @@ struct Geom {
 
     bool matches(u64 a, u64 b) const { return a == la && b == lb; }
     bool split() const { return block != 0; }
-    u64 spec_words(bool square) const { return (u64)(square ? 1 : 2) * np * ((u64)1 << log_t); }
-    // residues and carry flags of one product of this geometry (one block if split)
+    u64 spec_words(bool square) const { return np ? (u64)(square ? 1 : 2) * np * ((u64)1 << log_t) : 0; }
+    // Scratch of one product or convolution: [head][residues][tail]. The head holds
+    // a convolution's admission votes (launch.h; at offset 0 whatever the shape), the
+    // tail a product's carry flags.
+    u64 head_bytes() const { return conv ? (kAdmitBytes + 255) & ~(u64)255 : 0; }
+    // residues (0 for a schoolbook convolution)
+    u64 spec_bytes(bool square) const { return (spec_words(square) * 4 + 255) & ~(u64)255; }
+    u64 tail_bytes(u64 out) const { return conv ? 0 : (carry_scratch_bytes(out) + 255) & ~(u64)255; }
+    // scratch of one product of this geometry (one block if split)
     u64 member_bytes(bool square) const {
-        const u64 spec = (spec_words(square) * 4 + 255) & ~(u64)255;
         const u64 out = split() ? block + std::min(la, lb) : out_len;
-        return spec + ((conv ? 0 : carry_scratch_bytes(out)) + 255 & ~(u64)255);
+        return head_bytes() + spec_bytes(square) + tail_bytes(out);
     }
     // blocks per enqueue of a split product: bounded launch grids and arena
     u64 split_chunk() const {
@@ -68,11 +74,9 @@ struct Geom {
     u64 split_odd_bytes() const { return (out_len * 8 + 255) & ~(u64)255; }
     u64 split_flag_bytes() const { return (carry_scratch_bytes(out_len) + 255) & ~(u64)255; }
     u64 scratch_bytes(bool square) const {
-        if (conv && schoolbook) return 0;
         if (split())
             return split_desc_bytes() + split_odd_bytes() + split_flag_bytes() + split_chunk() * member_bytes(false);
-        const u64 spec = (spec_words(square) * 4 + 255) & ~(u64)255;
-        return spec + (conv ? 0 : carry_scratch_bytes(out_len));
+        return member_bytes(square);
     }
 };
 
@@ -95,11 +99,20 @@ bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp);
 // ---------------------------------------------------------------------------------
 // Enqueue (exec.cu)
 
-// The kernels of n batch members of one transform class, descriptors in device memory.
-bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st);
-// One product or convolution on `st`; b_ready (optional) completes when operand b is in place.
+// The kernels of n batch members of one transform class, descriptors in device
+// memory; convolution members are admitted on the device (their votes).
+// status: the failure bytes of launch.h, or null.
+bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st,
+                 u32* status = nullptr);
+// One product or convolution on `st`; b_ready (optional) completes when operand b
+// is in place. status: the failure bytes of launch.h, or null. admit: check a
+// convolution's coefficient bounds on the device first (device-pointer calls; the
+// host-pointer calls check them on the host).
 bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst, void* scratch,
-             cudaStream_t st, cudaEvent_t b_ready = nullptr);
+             cudaStream_t st, cudaEvent_t b_ready = nullptr, u32* status = nullptr, bool admit = false);
+// Test hook (ntt_debug_stall_lookback): true when the next look-back CRT launch
+// should start with its tile counter at 1, so that tile 0 never publishes.
+bool take_injected_stall();
 // Every coefficient within the plan's bound (magnitude bound when signed).
 bool coefficients_admitted(const Geom& g, const u64* v, u64 n, u64 max);
 

@@ -60,6 +60,8 @@ struct ProductDesc {
     uint8_t* agg;      // CRT look-back flags of a product (carry_flag_words u32), or null
     u32 square;
     u32 stride;        // convolution limbs per coefficient
+    u64 max_a, max_b;  // convolution coefficient bounds (magnitudes when signed)
+    u32* votes;        // admission votes of a convolution (kAdmitSlots u32), or null
 };
 
 // Operands and geometry of one transform-domain product. With `batch` set, the
@@ -83,6 +85,12 @@ struct TransformArgs {
     u32 flag_words;
     u64* dst;          // product limbs of the fused one-kernel path (single member)
     u64 out_len;
+    // Coefficient admission of a convolution by the one-CTA transform (the prime-0
+    // CTA checks the coefficients it loads and writes the votes): votes (null: no
+    // check) and bounds; batch members take theirs from the descriptors.
+    u32* votes;
+    u64 max_a, max_b;
+    int admit;         // batch: check the members' coefficients (their votes)
     PrimeSet ps;
 };
 
@@ -111,19 +119,48 @@ cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cuda
 cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st);
 cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st);
 
+// Failure status of the calls of a workspace or batch: four bytes in page-locked
+// host memory that the kernels reach through its device address (null: none). A
+// kernel that fails sets its byte to 1; the host reads the bytes after the call's
+// stream completes. Byte 0: a carry look-back wait gave up; byte 1: a convolution
+// coefficient exceeded its bound (the result was not written).
+constexpr u32 kStatusLookback = 1, kStatusBound = 2;
+__device__ __forceinline__ void report_status(u32* status, int byte) {
+    if (status) {
+        reinterpret_cast<volatile uint8_t*>(status)[byte] = 1;
+        __threadfence_system();
+    }
+}
+
+// Device-side coefficient admission of a convolution (src/convolve.rs:169-184):
+// kAdmitSlots CTAs scan the operands and each writes one vote (1: some coefficient
+// it saw exceeds its bound, 0: none), so every vote is rewritten by every check and
+// nothing needs clearing. The kernels that write the result skip the write when any
+// vote is 1.
+constexpr int kAdmitSlots = 128;
+constexpr u64 kAdmitBytes = 4 * kAdmitSlots;
+
 cudaError_t launch_crt_mul(const u32* resid, int log_t, u64 conv_len, u64 out_len, u64* dst,
                            uint8_t* agg, const CrtParams& cp, cudaStream_t st,
-                           void (*mark)(cudaStream_t) = nullptr);
+                           void (*mark)(cudaStream_t) = nullptr, u32* status = nullptr);
 cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst, bool sign,
-                            const CrtParams& cp, cudaStream_t st);
+                            const CrtParams& cp, cudaStream_t st, const u32* votes = nullptr,
+                            u32* status = nullptr);
 // Batched forms: every member of `batch` (device array of `count` descriptors)
-// shares log_t and the prime set of `cp`.
+// shares log_t and the prime set of `cp`. Convolution members with votes are
+// written only when admitted.
 cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_tiles, int log_t,
-                                 const CrtParams& cp, cudaStream_t st);
+                                 const CrtParams& cp, cudaStream_t st, u32* status = nullptr);
 cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
-                                  const CrtParams& cp, cudaStream_t st);
+                                  const CrtParams& cp, cudaStream_t st, u32* status = nullptr);
+// Admission votes of one convolution (votes: kAdmitSlots u32), or of every member
+// of a batch class (into each member's votes).
+cudaError_t launch_conv_admit(const u64* a, u64 la, const u64* b, u64 lb, u64 max_a, u64 max_b, bool sign,
+                              u32* votes, cudaStream_t st);
+cudaError_t launch_conv_admit_batch(const ProductDesc* batch, int count, bool sign, cudaStream_t st);
 // dst[0, len) += add[0, len) with carries (flags: carry_flag_words(len), zeroed).
-cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st);
+cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st,
+                             u32* status = nullptr);
 // Member descriptors of blocks first .. first + count - 1 of a split product
 // (block m of a times b into dst or odd at limb m * block; member m's residues and
 // flags at arena + (m - first) * member_bytes, flags spec_bytes in).
@@ -131,7 +168,8 @@ cudaError_t launch_split_descs(ProductDesc* d, u64 first, u64 count, const u64* 
                                u64 block, u64* dst, u64* odd, uint8_t* arena, u64 member_bytes, u64 spec_bytes,
                                cudaStream_t st);
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
-                                   int stride, bool sign, cudaStream_t st);
+                                   int stride, bool sign, cudaStream_t st, const u32* votes = nullptr,
+                                   u32* status = nullptr);
 // Four-step factor tables of one prime and transform length, built on the GPU:
 // every entry is a power of w (forward) or w^-1 (inverse) with its Shoup companion,
 // computed from the squares w^(2^i) (with companions) given here.

@@ -26,6 +26,7 @@
 //    do not matter.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -58,7 +59,7 @@ static __device__ __align__(256) uint2 g_noalloc_roots[kNaRootEntries];
 namespace {
 
 struct NoAllocDevice {
-    bool ready = false;
+    std::atomic<bool> ready{false};  // set (release) once scratch and roots are valid
     u32* scratch = nullptr;
     uint2* roots = nullptr;
 };
@@ -184,12 +185,17 @@ bool na_fail(const char* msg) {
 }
 
 // One-time set-up of the current device: device addresses of the static arrays
-// and the root tables copied into them.
+// and the root tables copied into them. After it, a call only reads the ready flag
+// (no lock).
 bool na_setup(int dev, NoAllocDevice*& out) {
-    std::lock_guard<std::mutex> lock(g_na_mutex);
     if (dev < 0 || dev >= 64) return na_fail("device index out of range");
     NoAllocDevice& d = g_na_device[dev];
-    if (!d.ready) {
+    if (d.ready.load(std::memory_order_acquire)) {
+        out = &d;
+        return true;
+    }
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!d.ready.load(std::memory_order_relaxed)) {
         na_build_constants();
         void* scratch = nullptr;
         void* roots = nullptr;
@@ -210,7 +216,7 @@ bool na_setup(int dev, NoAllocDevice*& out) {
         }
         d.scratch = (u32*)scratch;
         d.roots = (uint2*)roots;
-        d.ready = true;
+        d.ready.store(true, std::memory_order_release);
     }
     out = &d;
     return true;

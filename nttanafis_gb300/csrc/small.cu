@@ -27,13 +27,32 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     const PrimeParams& pp = g.ps.pr[blockIdx.x];
     const Member m = member_of(g, blockIdx.y, SQUARE);
     if (blockIdx.x == 0) clear_flags(g, blockIdx.y);
+    // convolutions: the prime-0 CTA checks every coefficient's bound as it loads it
+    u32* votes = g.votes;
+    u64 max_a = g.max_a, max_b = g.max_b;
+    if (g.batch) {
+        const ProductDesc& d = g.batch[blockIdx.y];
+        votes = g.admit ? d.votes : nullptr;
+        max_a = d.max_a;
+        max_b = d.max_b;
+    }
+    const bool check = votes && blockIdx.x == 0;
+    int bad = 0;
     u32* sa = sm;
     u32* sb = sm + VS;
     for (int i = threadIdx.x; i < N; i += kThreads) {
-        sa[pad_index(i)] = (u64)i < m.la ? reduce_coefficient<A, SIGNED>(__ldg(m.a + i), pp) : 0u;
-        if (!SQUARE) sb[pad_index(i)] = (u64)i < m.lb ? reduce_coefficient<A, SIGNED>(__ldg(m.b + i), pp) : 0u;
+        const u64 x = (u64)i < m.la ? __ldg(m.a + i) : 0;
+        sa[pad_index(i)] = reduce_coefficient<A, SIGNED>(x, pp);
+        if (check) bad |= coefficient_over<SIGNED>(x, max_a);
+        if (!SQUARE) {
+            const u64 y = (u64)i < m.lb ? __ldg(m.b + i) : 0;
+            sb[pad_index(i)] = reduce_coefficient<A, SIGNED>(y, pp);
+            if (check) bad |= coefficient_over<SIGNED>(y, max_b);
+        }
     }
-    __syncthreads();
+    bad = __syncthreads_or(bad);
+    if (check)  // every vote is written: vote 0 carries the verdict
+        for (int i = threadIdx.x; i < kAdmitSlots; i += kThreads) votes[i] = i == 0 && bad ? 1u : 0u;
     dif_full<A, LOG_N, kThreads, SQUARE ? 1 : 2, VS>(sm, pp.fwd, pp.p);
     for (int i = threadIdx.x; i < N; i += kThreads) {
         const int k = pad_index(i);

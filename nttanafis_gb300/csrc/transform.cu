@@ -250,10 +250,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, false);
     release_dependents();
-    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
     const int log_c = g.log_c;
     const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
     wait_prior_grid();  // the row pass's output
+    // the CRT look-back flags of this product, cleared once every kernel before
+    // this one has completed
+    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
     u32* const spec = m.spec + ((size_t)prime << g.log_t) + blockIdx.x * G + c;
     // Pass 1: levels 0-4 on rows 32 blk + k (bit-reversed spectrum in).
     {
@@ -420,7 +422,6 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, false);
     release_dependents();
-    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
     const u64 step = (u64)M::RS << g.log_c;
     u32* const base = m.spec + ((size_t)prime << g.log_t) + ((u64)M::row0() << g.log_c) +
                       (blockIdx.x << M::LOG_G) + M::col();
@@ -428,6 +429,7 @@ __global__ void NTT_COLS_BOUNDS k_inv_cols(const __grid_constant__ TransformArgs
     uint2* tw = reinterpret_cast<uint2*>(sm + M::G * M::VS);
     load_table<LOG_R>(tw, pp.inv);
     wait_prior_grid();  // the row pass's output
+    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);  // after every earlier kernel
     u32* q = base;
 #pragma unroll 1
     for (int k0 = 0; k0 < M::SWEEPS; k0 += B) {

@@ -18,6 +18,13 @@ __device__ __forceinline__ u32 reduce_coefficient(u64 x, const PrimeParams& pp) 
     return SIGNED ? reduce_signed<A>(x, pp) : reduce_limb<A>(x, pp);
 }
 
+// A convolution coefficient above its bound (its magnitude when signed).
+template <bool SIGNED>
+__device__ __forceinline__ int coefficient_over(u64 x, u64 mx) {
+    if (SIGNED) return ((int64_t)x < 0 ? (u64)0 - x : x) > mx;
+    return x > mx;
+}
+
 // Operands of the launch member a CTA works on (TransformArgs::batch).
 struct Member {
     const u64* a;

@@ -12,8 +12,8 @@ ROOT = Path(__file__).resolve().parents[1]
 MASK = (1 << 64) - 1
 
 
-def declared_symbols():
-    text = (ROOT / "include" / "ntt_gb300.h").read_text()
+def declared_symbols(header: str = "ntt_gb300.h"):
+    text = (ROOT / "include" / header).read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(ntt_[a-z0-9_]+)\s*\(", text)))
 
@@ -25,6 +25,18 @@ def test_library_exports_every_declared_symbol():
     for name in names:
         assert hasattr(lib, name), name
     assert sorted(ntt.exported_symbols()) == names
+
+
+def test_probe_library_is_separate_and_exports_its_header():
+    from nttanafis_gb300 import probe
+
+    lib = probe.library()
+    names = declared_symbols("ntt_probe.h")
+    for name in names:
+        assert hasattr(lib, name), name
+    assert sorted(probe.exported_symbols()) == names
+    assert not set(names) & set(declared_symbols())  # nothing of it in the product ABI
+    assert lib.ntt_probe_variants() == len(probe.VARIANTS)
 
 
 def test_version_and_counters():
@@ -55,9 +67,12 @@ def test_conv_plans_reject_like_the_reference(golden):
     for la, lb, ma, mb, s in golden["rejections"]["conv_none"]:
         assert ntt.ConvPlan.new(la, lb, ma, mb, bool(s)) is None
     p = ntt.ConvPlan.new(3, 2, 3, 5, False)
-    assert p.output_len() == 4 and p.scratch_len() == 0 and p.schoolbook
+    # the reference's schoolbook plans need no scratch for their arithmetic
+    # (src/convolve.rs:132); the device call's scratch holds only the 512 bytes of
+    # the on-device admission votes, in front of the residues of transform plans
+    assert p.output_len() == 4 and p.schoolbook and p.scratch_len() == 64
     big = ntt.ConvPlan.new(30, 30, 7, 7, False)
-    assert big.scratch_len() > 0 and not big.schoolbook
+    assert big.scratch_len() > 64 and not big.schoolbook
 
 
 def test_conv_plan_matches_oracle_stride_and_output():

@@ -247,8 +247,12 @@ def test_conv_device_paths(gpu):
 def test_butterfly_probe_and_launch_counter(gpu):
     # the compute-ceiling probe runs (positive, plausible rate) and the launch
     # counter grows by the kernels a product enqueues
-    rate = gpu.butterfly_rate(152, 50)
+    from nttanafis_gb300 import probe
+
+    rate = probe.butterfly_rate(152, 50)
     assert 1e11 < rate < 1e14
+    for v in range(len(probe.VARIANTS)):
+        assert probe.rate(v, 152, 20) > 1e9, probe.VARIANTS[v]
     import torch
 
     ws = gpu.GpuMulWorkspace()

@@ -220,11 +220,16 @@ def test_wide_prime_class_2_pow_24(ws):
     assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
 
 
-def test_config_16m_mul_and_sqr_fingerprints(ws):
+def test_config_16m_mul_and_sqr_exact(ws, golden):
+    # bit-exact against the oracle's digests (tests/golden/make_big_digests.py),
+    # with the Mersenne fingerprints as a second, independent check
+    cases = {c["kind"]: c for c in golden["big_products"]["cases"]}
     a, b = operand(1 << 24, 1), operand(1 << 24, 2)
     c = gpu_mul(ws, a, b, extra=1)
+    assert hashlib.sha256(c.astype("<u8").tobytes()).hexdigest() == cases["mul"]["sha256"]
     assert fingerprint_ok(a, b, c)
     s = gpu_sqr(ws, a)
+    assert hashlib.sha256(s.astype("<u8").tobytes()).hexdigest() == cases["sqr"]["sha256"]
     assert fingerprint_ok(a, a, s)
 
 

@@ -65,3 +65,36 @@ def test_noalloc_refuses_shapes_above_its_limit(gpu):
     assert "4096" in gpu.last_error()
     torch.cuda.synchronize()
     assert bool((dst == 7).all())
+
+
+def test_noalloc_edge_shapes(gpu):
+    # an empty operand (zeros, no kernel), the smallest transform (1 x 1 and 3 x 5),
+    # and all-ones operands at the limit, whose carries cross every CRT tile; each
+    # bit for bit against the workspace call, the limb past the result untouched
+    import torch
+
+    lib = gpu.library()
+    ws = gpu.GpuMulWorkspace()
+    stream = torch.cuda.current_stream()
+    handle = stream.cuda_stream
+    empty = torch.empty(0, dtype=torch.int64, device="cuda")
+    b = _device_limbs(torch, np.arange(1, 8, dtype=np.uint64))
+    got = torch.full((8,), -1, dtype=torch.int64, device="cuda")
+    assert lib.ntt_mul_noalloc_device(got.data_ptr(), 8, empty.data_ptr(), 0, b.data_ptr(), 7, handle) == 1
+    torch.cuda.synchronize()
+    assert bool((got[:7] == 0).all()) and int(got[7]) == -1
+    ones = np.full(2049, 0xFFFFFFFFFFFFFFFF, dtype=np.uint64)
+    from nttanafis_gb300.operands import operand
+
+    for a_h, b_h in [(operand(1, 5), operand(1, 6)), (operand(3, 7), operand(5, 8)), (ones[:2048], ones)]:
+        a, b = _device_limbs(torch, a_h), _device_limbs(torch, b_h)
+        n = a_h.size + b_h.size
+        expected = torch.full((n + 1,), -1, dtype=torch.int64, device="cuda")
+        got = torch.full((n + 1,), -1, dtype=torch.int64, device="cuda")
+        assert ws.mul_device(expected, a, b, stream), gpu.last_error()
+        ok = lib.ntt_mul_noalloc_device(got.data_ptr(), n, a.data_ptr(), a_h.size, b.data_ptr(), b_h.size, handle)
+        assert ok == 1, gpu.last_error()
+        torch.cuda.synchronize()
+        assert torch.equal(got, expected), (a_h.size, b_h.size)
+        assert int(got[n]) == -1
+    ws.close()
