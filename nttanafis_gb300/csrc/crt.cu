@@ -25,11 +25,11 @@ namespace ntt {
 // Coefficient k of a residue array [prime][T] as four u64 words.
 template <int NP>
 __device__ __forceinline__ void crt_coeff(const u32* __restrict__ resid, int log_t, u64 k,
-                                          const CrtParams& cp, u64 out[4]) {
+                                          const CrtParams& cp, const u32 (*qp)[kQpStride], u64 out[4]) {
     u32 r[NP], x[NP + 1];
 #pragma unroll
     for (int i = 0; i < NP; ++i) r[i] = __ldg(resid + ((size_t)i << log_t) + k);
-    crt_words<NP>(r, cp, x);
+    crt_words<NP>(r, cp, qp, x);
     u64 w[4];
     pack_words<NP, 4>(x, w);
 #pragma unroll
@@ -137,7 +137,9 @@ __global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restric
     // tiles whose CTAs are already running.
     __shared__ u32 s_tile;
     __shared__ u64 s_pre[L][L];  // the L coefficients before the tile
+    __shared__ u32 s_qp[kMaxPrimes + 1][kQpStride];
     if (threadIdx.x == 0) s_tile = atomicAdd(&flags[0], 1u);
+    stage_multiples(cp, s_qp);
     __syncthreads();
     const u32 tile = s_tile;
     const u32 tiles = (u32)((out_len + kCrtTile - 1) / kCrtTile);
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restric
 #pragma unroll
         for (int c = 0; c < kCrtPer; ++c) {
             u32 x[NP + 1];
-            crt_words<NP>(r[c], cp, x);
+            crt_words<NP>(r[c], cp, s_qp, x);
             pack_words<NP, L>(x, cw[c]);
         }
     }
@@ -178,7 +180,7 @@ __global__ void __launch_bounds__(kCrtThreads, 5) k_crt_mul(const u32* __restric
             u32 r[NP], x[NP + 1];
 #pragma unroll
             for (int i = 0; i < NP; ++i) r[i] = __ldg(resid + ((size_t)i << log_t) + k);
-            crt_words<NP>(r, cp, x);
+            crt_words<NP>(r, cp, s_qp, x);
             pack_words<NP, L>(x, w);
         }
 #pragma unroll
@@ -244,11 +246,11 @@ __global__ void k_split_descs(ProductDesc* __restrict__ d, u64 first, u64 count,
 
 // Whether a convolution may be written: false when any admission vote is set
 // (votes: kAdmitSlots words, or null when the coefficients were admitted on the
-// host). Every thread of the CTA calls it (one barrier).
+// host). Every thread of the CTA calls it: it holds one barrier in either case.
 __device__ __forceinline__ bool admitted(const u32* __restrict__ votes) {
-    if (!votes) return true;
     int bad = 0;
-    for (int i = threadIdx.x; i < kAdmitSlots; i += blockDim.x) bad |= __ldcg(votes + i) != 0u;
+    if (votes)
+        for (int i = threadIdx.x; i < kAdmitSlots; i += blockDim.x) bad |= __ldcg(votes + i) != 0u;
     return !__syncthreads_or(bad);
 }
 
@@ -317,6 +319,8 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict_
         votes = d.votes;
     }
     if ((u64)blockIdx.x * blockDim.x >= conv_len) return;
+    __shared__ u32 s_qp[kMaxPrimes + 1][kQpStride];
+    stage_multiples(cp, s_qp);  // published by the barrier in admitted()
     if (!admitted(votes)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) report_status(status, 1);
         return;
@@ -324,7 +328,7 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_conv(const u32* __restrict_
     const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= conv_len) return;
     u64 w[4];
-    crt_coeff<NP>(resid, log_t, k, cp, w);
+    crt_coeff<NP>(resid, log_t, k, cp, s_qp, w);
     const u64 fill = (w[3] >> 63) ? ~0ull : 0ull;
     u64* out = dst + k * (u64)stride;
     out[0] = w[0];

@@ -9,21 +9,24 @@ namespace ntt {
 
 constexpr int kCrtThreads = kCrtTile / 4;
 
-// Reconstructs X from its residues r_i: returns the NP + 1 u32 words (two's
-// complement) of X = S - q*P, S = sum_i y_i*(P/p_i), y_i = r_i*(P/p_i)^-1 mod p_i,
-// q rounded from sum_i y_i/p_i. Unsigned: 0 <= X < P/2. Signed: |X| <= P/4.
+// The multiples q * P (q = 0..np) of a prime set, staged in shared memory by the
+// CRT kernels: every thread calls it, a barrier of the caller publishes it.
+__device__ __forceinline__ void stage_multiples(const CrtParams& cp, u32 (*qp)[kQpStride]) {
+    for (int i = threadIdx.x; i < (kMaxPrimes + 1) * kQpStride; i += blockDim.x)
+        qp[i / kQpStride][i % kQpStride] = cp.qP[i / kQpStride][i % kQpStride];
+}
+
+// Reconstructs X from its residues y_i = r_i*(P/p_i)^-1 mod p_i (canonical; the
+// transforms fold the cofactor inverse into their scale): returns the NP + 1 u32
+// words (two's complement) of X = S - q*P, S = sum_i y_i*(P/p_i), q rounded from
+// sum_i y_i/p_i and q*P read from the staged multiples. Unsigned: 0 <= X < P/2.
+// Signed: |X| <= P/4.
 template <int NP>
-__device__ __forceinline__ void crt_words(const u32 (&r)[NP], const CrtParams& cp, u32 (&x)[NP + 1]) {
-    u32 y[NP];
+__device__ __forceinline__ void crt_words(const u32 (&y)[NP], const CrtParams& cp, const u32 (*qp)[kQpStride],
+                                          u32 (&x)[NP + 1]) {
     float f = 0.0f;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const u32 p = cp.p[i];
-        u32 v = shoup_mul(r[i], cp.inv[i].x, cp.inv[i].y, p);
-        v = sub_if_ge(v, p);
-        y[i] = v;
-        f = fmaf((float)v, cp.pinv[i], f);
-    }
+    for (int i = 0; i < NP; ++i) f = fmaf((float)y[i], cp.pinv[i], f);
     // S = sum_i y_i * M_i in NP + 1 words (the top word stays zero), by carry
     // chains: the low halves of y_i * M_i[w] into word w, the high halves into w+1.
     u32 S[NP + 1];
@@ -32,12 +35,10 @@ __device__ __forceinline__ void crt_words(const u32 (&r)[NP], const CrtParams& c
 #pragma unroll
     for (int i = 0; i < NP; ++i) CrtChains<NP>::accumulate(S, y[i], cp.M[i]);
     // X = S - q*P in NP + 1 words; the top word is the sign (0 or all ones).
-    const u32 q = (u32)(f + cp.bias);
+    const u32 q = min((u32)(f + cp.bias), (u32)NP);
     u32 U[NP + 1];
 #pragma unroll
-    for (int w = 0; w < NP; ++w) U[w] = q * cp.P[w];
-    U[NP] = 0;
-    CrtChains<NP>::high_products(U, q, cp.P);
+    for (int w = 0; w <= NP; ++w) U[w] = qp[q][w];
     CrtChains<NP>::subtract(x, S, U);
 }
 

@@ -18,12 +18,6 @@ struct CrtChains<1> {
         : "+r"(S[0]), "+r"(S[1])
         : "r"(y), "r"(M[0]));
     }
-    static __device__ __forceinline__ void high_products(u32 (&U)[2], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %1, %2, %0;\n\t"
-        : "+r"(U[1])
-        : "r"(q), "r"(P[0]));
-    }
     static __device__ __forceinline__ void subtract(u32 (&x)[2], const u32 (&S)[2], const u32 (&U)[2]) {
         asm(
         "sub.cc.u32 %0, %2, %4;\n\t"
@@ -44,13 +38,6 @@ struct CrtChains<2> {
         "addc.u32 %2, %2, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2])
         : "r"(y), "r"(M[0]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[3], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %2, %3, %0;\n\t"
-        "madc.hi.u32 %1, %2, %4, %1;\n\t"
-        : "+r"(U[1]), "+r"(U[2])
-        : "r"(q), "r"(P[0]), "r"(P[1]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[3], const u32 (&S)[3], const u32 (&U)[3]) {
         asm(
@@ -75,14 +62,6 @@ struct CrtChains<3> {
         "addc.u32 %3, %3, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2]), "+r"(S[3])
         : "r"(y), "r"(M[0]), "r"(M[1]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[4], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %3, %4, %0;\n\t"
-        "madc.hi.cc.u32 %1, %3, %5, %1;\n\t"
-        "madc.hi.u32 %2, %3, %6, %2;\n\t"
-        : "+r"(U[1]), "+r"(U[2]), "+r"(U[3])
-        : "r"(q), "r"(P[0]), "r"(P[1]), "r"(P[2]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[4], const u32 (&S)[4], const u32 (&U)[4]) {
         asm(
@@ -110,15 +89,6 @@ struct CrtChains<4> {
         "addc.u32 %4, %4, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2]), "+r"(S[3]), "+r"(S[4])
         : "r"(y), "r"(M[0]), "r"(M[1]), "r"(M[2]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[5], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %4, %5, %0;\n\t"
-        "madc.hi.cc.u32 %1, %4, %6, %1;\n\t"
-        "madc.hi.cc.u32 %2, %4, %7, %2;\n\t"
-        "madc.hi.u32 %3, %4, %8, %3;\n\t"
-        : "+r"(U[1]), "+r"(U[2]), "+r"(U[3]), "+r"(U[4])
-        : "r"(q), "r"(P[0]), "r"(P[1]), "r"(P[2]), "r"(P[3]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[5], const u32 (&S)[5], const u32 (&U)[5]) {
         asm(
@@ -149,16 +119,6 @@ struct CrtChains<5> {
         "addc.u32 %5, %5, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2]), "+r"(S[3]), "+r"(S[4]), "+r"(S[5])
         : "r"(y), "r"(M[0]), "r"(M[1]), "r"(M[2]), "r"(M[3]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[6], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %5, %6, %0;\n\t"
-        "madc.hi.cc.u32 %1, %5, %7, %1;\n\t"
-        "madc.hi.cc.u32 %2, %5, %8, %2;\n\t"
-        "madc.hi.cc.u32 %3, %5, %9, %3;\n\t"
-        "madc.hi.u32 %4, %5, %10, %4;\n\t"
-        : "+r"(U[1]), "+r"(U[2]), "+r"(U[3]), "+r"(U[4]), "+r"(U[5])
-        : "r"(q), "r"(P[0]), "r"(P[1]), "r"(P[2]), "r"(P[3]), "r"(P[4]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[6], const u32 (&S)[6], const u32 (&U)[6]) {
         asm(
@@ -192,17 +152,6 @@ struct CrtChains<6> {
         "addc.u32 %6, %6, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2]), "+r"(S[3]), "+r"(S[4]), "+r"(S[5]), "+r"(S[6])
         : "r"(y), "r"(M[0]), "r"(M[1]), "r"(M[2]), "r"(M[3]), "r"(M[4]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[7], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %6, %7, %0;\n\t"
-        "madc.hi.cc.u32 %1, %6, %8, %1;\n\t"
-        "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
-        "madc.hi.cc.u32 %3, %6, %10, %3;\n\t"
-        "madc.hi.cc.u32 %4, %6, %11, %4;\n\t"
-        "madc.hi.u32 %5, %6, %12, %5;\n\t"
-        : "+r"(U[1]), "+r"(U[2]), "+r"(U[3]), "+r"(U[4]), "+r"(U[5]), "+r"(U[6])
-        : "r"(q), "r"(P[0]), "r"(P[1]), "r"(P[2]), "r"(P[3]), "r"(P[4]), "r"(P[5]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[7], const u32 (&S)[7], const u32 (&U)[7]) {
         asm(
@@ -239,18 +188,6 @@ struct CrtChains<7> {
         "addc.u32 %7, %7, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2]), "+r"(S[3]), "+r"(S[4]), "+r"(S[5]), "+r"(S[6]), "+r"(S[7])
         : "r"(y), "r"(M[0]), "r"(M[1]), "r"(M[2]), "r"(M[3]), "r"(M[4]), "r"(M[5]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[8], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %7, %8, %0;\n\t"
-        "madc.hi.cc.u32 %1, %7, %9, %1;\n\t"
-        "madc.hi.cc.u32 %2, %7, %10, %2;\n\t"
-        "madc.hi.cc.u32 %3, %7, %11, %3;\n\t"
-        "madc.hi.cc.u32 %4, %7, %12, %4;\n\t"
-        "madc.hi.cc.u32 %5, %7, %13, %5;\n\t"
-        "madc.hi.u32 %6, %7, %14, %6;\n\t"
-        : "+r"(U[1]), "+r"(U[2]), "+r"(U[3]), "+r"(U[4]), "+r"(U[5]), "+r"(U[6]), "+r"(U[7])
-        : "r"(q), "r"(P[0]), "r"(P[1]), "r"(P[2]), "r"(P[3]), "r"(P[4]), "r"(P[5]), "r"(P[6]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[8], const u32 (&S)[8], const u32 (&U)[8]) {
         asm(
@@ -290,19 +227,6 @@ struct CrtChains<8> {
         "addc.u32 %8, %8, 0;\n\t"
         : "+r"(S[0]), "+r"(S[1]), "+r"(S[2]), "+r"(S[3]), "+r"(S[4]), "+r"(S[5]), "+r"(S[6]), "+r"(S[7]), "+r"(S[8])
         : "r"(y), "r"(M[0]), "r"(M[1]), "r"(M[2]), "r"(M[3]), "r"(M[4]), "r"(M[5]), "r"(M[6]));
-    }
-    static __device__ __forceinline__ void high_products(u32 (&U)[9], u32 q, const u32* P) {
-        asm(
-        "mad.hi.cc.u32 %0, %8, %9, %0;\n\t"
-        "madc.hi.cc.u32 %1, %8, %10, %1;\n\t"
-        "madc.hi.cc.u32 %2, %8, %11, %2;\n\t"
-        "madc.hi.cc.u32 %3, %8, %12, %3;\n\t"
-        "madc.hi.cc.u32 %4, %8, %13, %4;\n\t"
-        "madc.hi.cc.u32 %5, %8, %14, %5;\n\t"
-        "madc.hi.cc.u32 %6, %8, %15, %6;\n\t"
-        "madc.hi.u32 %7, %8, %16, %7;\n\t"
-        : "+r"(U[1]), "+r"(U[2]), "+r"(U[3]), "+r"(U[4]), "+r"(U[5]), "+r"(U[6]), "+r"(U[7]), "+r"(U[8])
-        : "r"(q), "r"(P[0]), "r"(P[1]), "r"(P[2]), "r"(P[3]), "r"(P[4]), "r"(P[5]), "r"(P[6]), "r"(P[7]));
     }
     static __device__ __forceinline__ void subtract(u32 (&x)[9], const u32 (&S)[9], const u32 (&U)[9]) {
         asm(

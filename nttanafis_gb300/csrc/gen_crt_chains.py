@@ -45,22 +45,6 @@ def accumulate(np_: int) -> str:
             f"        asm(\n{body}\n        : {outs}\n        : {ins});\n    }}\n")
 
 
-def high_products(np_: int) -> str:
-    """U[1..NP] += high halves of q * P[0..NP-1] (U[w] holds the low half of q*P[w])."""
-    u = lambda w: f"%{w - 1}"        # U[1..NP]: operands 0..NP-1
-    q = f"%{np_}"
-    p = lambda w: f"%{np_ + 1 + w}"  # P[w]
-    lines = [f"mad.hi.cc.u32 {u(1)}, {q}, {p(0)}, {u(1)};"]
-    for w in range(2, np_ + 1):
-        op = "madc.hi.cc.u32" if w < np_ else "madc.hi.u32"
-        lines.append(f"{op} {u(w)}, {q}, {p(w - 1)}, {u(w)};")
-    outs = ", ".join(f'"+r"(U[{w}])' for w in range(1, np_ + 1))
-    ins = ", ".join(['"r"(q)'] + [f'"r"(P[{w}])' for w in range(np_)])
-    body = "\n".join(f'        "{l}\\n\\t"' for l in lines)
-    return (f"    static __device__ __forceinline__ void high_products(u32 (&U)[{np_ + 1}], u32 q, const u32* P) {{\n"
-            f"        asm(\n{body}\n        : {outs}\n        : {ins});\n    }}\n")
-
-
 def subtract(np_: int) -> str:
     """x[0..NP] = S[0..NP] - U[0..NP] with borrows."""
     n = np_ + 1
@@ -89,7 +73,6 @@ def main() -> None:
     for np_ in range(1, MAX_PRIMES + 1):
         parts.append(f"template <>\nstruct CrtChains<{np_}> {{\n")
         parts.append(accumulate(np_))
-        parts.append(high_products(np_))
         parts.append(subtract(np_))
         parts.append("};\n\n")
     parts.append("}  // namespace ntt\n")

@@ -94,18 +94,33 @@ struct TransformArgs {
     PrimeSet ps;
 };
 
-// Exact-CRT constants of one prime set (words in radix 2^32).
+// Exact-CRT constants of one prime set (words in radix 2^32). The transforms fold
+// each prime's (P/p_i)^-1 into their inverse scale, so the residues the CRT reads
+// are already y_i = r_i * (P/p_i)^-1 mod p_i.
+constexpr int kQpStride = kMaxPrimes + 2;  // odd row stride: conflict-free rows
 struct CrtParams {
     int np;
     int l64;                           // u64 words of one reconstructed coefficient
     int stride;                        // output limbs per coefficient (convolutions)
     float bias;                        // 0.25 unsigned, 0.5 signed quotient rounding
     u32 p[kMaxPrimes];
-    uint2 inv[kMaxPrimes];             // (P/p_i)^-1 mod p_i with Shoup companion
     float pinv[kMaxPrimes];            // 1/p_i in fp32
     u32 M[kMaxPrimes][kMaxPrimes];     // P/p_i
     u32 P[kMaxPrimes];                 // P
+    u32 qP[kMaxPrimes + 1][kQpStride]; // q * P for q = 0..np (np + 1 words each)
 };
+
+// q * P of a prime set for q = 0..np into cp.qP (host side).
+inline void fill_multiples(CrtParams& cp) {
+    for (int q = 0; q <= cp.np; ++q) {
+        u64 carry = 0;
+        for (int w = 0; w <= cp.np; ++w) {
+            const u64 t = (u64)q * (w < cp.np ? cp.P[w] : 0u) + carry;
+            cp.qP[q][w] = (u32)t;
+            carry = t >> 32;
+        }
+    }
+}
 
 // Launchers; each returns the launch status.
 cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st);

@@ -143,8 +143,8 @@ void na_build_constants() {
         for (int w = mw - 1; w >= 0; --w) mmod = ((mmod << 32) | M[w]) % p;
         for (int w = 0; w < mw && w < kMaxPrimes; ++w) g_na_crt.M[i][w] = M[w];
         g_na_crt.p[i] = p;
-        g_na_crt.inv[i] = na_shoup(na_pow((u32)mmod, p - 2, p), p);
         g_na_crt.pinv[i] = 1.0f / (float)p;
+        const u32 cofactor = na_pow((u32)mmod, p - 2, p);  // (P/p_i)^-1, folded into the scale
 
         PrimeParams& pp = g_na_params[i];
         pp = PrimeParams{};
@@ -158,7 +158,7 @@ void na_build_constants() {
         pp.r32 = na_shoup(r32, p);
         for (int lt = 0; lt <= kNaLogT; ++lt) {
             const u32 tinv = na_pow((u32)(((u64)1 << lt) % p), p - 2, p);
-            g_na_scale[i][lt] = na_shoup(na_mulmod(tinv, r32, p), p);
+            g_na_scale[i][lt] = na_shoup(na_mulmod(na_mulmod(tinv, r32, p), cofactor, p), p);
         }
         const u32 g = na_generator(p);
         uint2* fwd = g_na_host_roots + (size_t)(2 * i) * kNaPoints;
@@ -176,6 +176,7 @@ void na_build_constants() {
             }
         }
     }
+    fill_multiples(g_na_crt);
     g_na_constants = true;
 }
 

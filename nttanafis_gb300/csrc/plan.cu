@@ -281,7 +281,7 @@ struct StepTables {
 
 static std::mutex g_table_mutex;
 static std::map<std::pair<int, u32>, PrimeTables> g_prime_tables;
-static std::map<std::tuple<int, u32, int, int>, StepTables> g_step_tables;
+static std::map<std::tuple<int, u32, int, int, u32>, StepTables> g_step_tables;
 static std::map<int, bool> g_device_ready;
 
 static uint2 shoup_pair(u32 w, u32 p) { return make_uint2(w, (u32)(((u64)w << 32) / p)); }
@@ -342,15 +342,19 @@ static cudaStream_t table_stream(int dev) {
 // Root tables of one transform length: the inverse scale and, for the four-step
 // sizes, the forward and inverse twiddle factors in the layouts the column and row
 // passes read (launch.h describes them), built by a kernel from the squares of w.
-static bool step_tables(int dev, u32 p, int log_t, int log_r, StepTables& out) {
-    auto key = std::make_tuple(dev, p, log_t, log_r);
+// `cofactor` is the prime's CRT factor (P/p)^-1 mod p of the prime set, folded into
+// the scale.
+static bool step_tables(int dev, u32 p, int log_t, int log_r, u32 cofactor, StepTables& out) {
+    auto key = std::make_tuple(dev, p, log_t, log_r, cofactor);
     auto it = g_step_tables.find(key);
     if (it != g_step_tables.end()) { out = it->second; return true; }
     const u32 g = generator(p);
     const u32 w = powmod(g, (p - 1) >> log_t, p);
     const u32 iw = invmod(w, p);
-    // Inverse scale: T^-1 times 2^32 (undoes the Montgomery pointwise product).
-    const u32 scale = mulmod(invmod((u32)(((u64)1 << log_t) % p), p), (u32)(((u64)1 << 32) % p), p);
+    // Inverse scale: T^-1 times 2^32 (undoes the Montgomery pointwise product) times
+    // the CRT cofactor inverse.
+    const u32 scale = mulmod(mulmod(invmod((u32)(((u64)1 << log_t) % p), p), (u32)(((u64)1 << 32) % p), p),
+                             cofactor, p);
     StepTables t;
     t.scale = shoup_pair(scale, p);
     if (log_r > 0) {
@@ -441,9 +445,13 @@ bool prepare_params(const Geom& g, int log_r, PrimeSet& ps, CrtParams& cp) {
     for (int w = 0; w < (int)P.size() && w < kMaxPrimes; ++w) cp.P[w] = P[w];
     for (int i = 0; i < g.np; ++i) {
         const u32 p = g.primes[i];
+        // CRT cofactor M_i = P / p_i and its inverse, which the inverse scale absorbs
+        Words M{1};
+        for (int j = 0; j < g.np; ++j) if (j != i) M = words_mul_small(M, g.primes[j]);
+        const u32 cofactor = invmod(words_mod(M, p), p);
         PrimeTables pt;
         StepTables st;
-        if (!prime_tables(dev, p, pt) || !step_tables(dev, p, g.log_t, log_r, st)) return false;
+        if (!prime_tables(dev, p, pt) || !step_tables(dev, p, g.log_t, log_r, cofactor, st)) return false;
         PrimeParams& pp = ps.pr[i];
         pp.p = p;
         u32 pinv = 1;  // p^-1 mod 2^32 by Newton's iteration (bits double each step)
@@ -474,14 +482,11 @@ bool prepare_params(const Geom& g, int log_r, PrimeSet& ps, CrtParams& cp) {
         pp.f4_b = st.f_b;
         pp.i4_lo = st.i_lo;
         pp.i4_hi = st.i_hi;
-        // CRT cofactors M_i = P / p_i and their inverses.
-        Words M{1};
-        for (int j = 0; j < g.np; ++j) if (j != i) M = words_mul_small(M, g.primes[j]);
         for (int w = 0; w < (int)M.size() && w < kMaxPrimes; ++w) cp.M[i][w] = M[w];
         cp.p[i] = p;
-        cp.inv[i] = shoup_pair(invmod(words_mod(M, p), p), p);
         cp.pinv[i] = 1.0f / (float)p;
     }
+    fill_multiples(cp);
     g_param_cache[key] = std::make_pair(ps, cp);
     return true;
 }

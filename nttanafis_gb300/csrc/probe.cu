@@ -16,6 +16,8 @@
 //   7  64-bit integer multiply (low word)   8  f64 FMA
 //   9  IMAD.WIDE (32 x 32 -> 64-bit multiply-add)   10  I2F (u32 -> f32 conversion,
 //      with one LOP3 each)
+// and two more forms of variant 0's butterfly, whose Shoup quotient is the high
+// word of a 32 x 32 -> 64-bit product: 11 PTX mul.wide, 12 a 64-bit product in C.
 // The result is a checksum, so no work can be dropped, and the milliseconds of the
 // timed launch (after one shorter warm-up launch).
 #include <cuda_runtime.h>
@@ -47,6 +49,29 @@ __device__ __forceinline__ void shoup64_dif(u64& x, u64& y, ulonglong2 w, u64 p)
     y = d * w.x - q * p;  // [0, 2p)
 }
 
+// The lazy Shoup butterfly with its quotient taken from the high word of a
+// 32 x 32 -> 64-bit multiply (PTX mul.wide) instead of a multiply-high.
+__device__ __forceinline__ void shoup_wide_dif(u32& x, u32& y, uint2 w, u32 p) {
+    const u32 p2 = p << 1;
+    const u32 s = x + y;
+    const u32 d = x - y + p2;
+    x = min(s, s - p2);
+    u64 t;
+    asm("mul.wide.u32 %0, %1, %2;" : "=l"(t) : "r"(d), "r"(w.y));
+    const u32 q = (u32)(t >> 32);
+    y = d * w.x - q * p;
+}
+
+// The same written as a 64-bit product in C, for the compiler's own choice.
+__device__ __forceinline__ void shoup_c64_dif(u32& x, u32& y, uint2 w, u32 p) {
+    const u32 p2 = p << 1;
+    const u32 s = x + y;
+    const u32 d = x - y + p2;
+    x = min(s, s - p2);
+    const u32 q = (u32)(((u64)d * w.y) >> 32);
+    y = d * w.x - q * p;
+}
+
 // The reference's exact product: h + l = d * w exactly (FMA), quotient from h,
 // remainder by FMA; residues stay in (-p, p).
 __device__ __forceinline__ void f64_dif(double& x, double& y, double w, double p, double pinv) {
@@ -61,7 +86,7 @@ __device__ __forceinline__ void f64_dif(double& x, double& y, double w, double p
 template <int V>
 __global__ void __launch_bounds__(256) k_probe(u64* __restrict__ out, u64 p, u64 w0, u64 wp0, int iters) {
     u64 acc = 0;
-    if constexpr (V <= 3) {
+    if constexpr (V <= 3 || V >= 11) {
         // T: residue type of the variant
         using T = typename std::conditional<V == 2, u64, typename std::conditional<V == 3, double, u32>::type>::type;
         T x[16];
@@ -90,6 +115,8 @@ __global__ void __launch_bounds__(256) k_probe(u64* __restrict__ out, u64 p, u64
                         if constexpr (V == 1) mont_dif(x[b + c], x[b + c + half], w32[c], (u32)p);
                         if constexpr (V == 2) shoup64_dif(x[b + c], x[b + c + half], w64[c], p);
                         if constexpr (V == 3) f64_dif(x[b + c], x[b + c + half], wf[c], pf, pinv);
+                        if constexpr (V == 11) shoup_wide_dif(x[b + c], x[b + c + half], w32[c], (u32)p);
+                        if constexpr (V == 12) shoup_c64_dif(x[b + c], x[b + c + half], w32[c], (u32)p);
                     }
             }
         }
@@ -141,12 +168,13 @@ void launch(int blocks, u64* out, u64 p, u64 w0, u64 wp0, int iters) {
 }
 
 using Launcher = void (*)(int, u64*, u64, u64, u64, int);
-constexpr Launcher kLaunchers[] = {launch<0>, launch<1>, launch<2>, launch<3>, launch<4>, launch<5>,
-                                   launch<6>, launch<7>, launch<8>, launch<9>, launch<10>};
+constexpr Launcher kLaunchers[] = {launch<0>, launch<1>, launch<2>,  launch<3>,  launch<4>,
+                                   launch<5>, launch<6>, launch<7>,  launch<8>,  launch<9>,
+                                   launch<10>, launch<11>, launch<12>};
 constexpr int kVariants = sizeof(kLaunchers) / sizeof(kLaunchers[0]);
 
 // Operations one thread performs per iteration of variant v.
-double ops_per_iter(int v) { return v <= 3 ? 32.0 : 64.0; }
+double ops_per_iter(int v) { return v <= 3 || v >= 11 ? 32.0 : 64.0; }
 
 }  // namespace
 

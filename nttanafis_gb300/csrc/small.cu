@@ -111,7 +111,9 @@ __global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant_
     __syncthreads();
     dit_full<A, LOG_N, kThreads, 1, VS>(sa, pp.inv, pp.p);
     for (int i = threadIdx.x; i < N; i += kThreads) sa[pad_index(i)] = A::canonical(sa[pad_index(i)], pp.p);
-    cluster.sync();  // every prime's residues are in place
+    __shared__ u32 s_qp[kMaxPrimes + 1][kQpStride];
+    stage_multiples(cp, s_qp);
+    cluster.sync();  // every prime's residues (and this CTA's multiples) are in place
     // CTA r reconstructs output tiles r, r + NP, ... (at most MT of them).
     constexpr int MT = ((N + kCrtTile) / kCrtTile + NP - 1) / NP;
     __shared__ u64 s_pre[L][L];
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant_
         u32 r[NP], x[NP + 1];
 #pragma unroll
         for (int i = 0; i < NP; ++i) r[i] = k < conv_len ? res[i][pad_index((int)k)] : 0u;
-        crt_words<NP>(r, cp, x);
+        crt_words<NP>(r, cp, s_qp, x);
         pack_words<NP, L>(x, w);
     };
     u64 sv[MT][kCrtPer];

@@ -179,9 +179,16 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
 // best.
 constexpr int kCol2LogR = 10;
 static_assert(col_group_log(10) == 3 && col_log_rs(10) == 5, "two-pass columns assume 8 columns per CTA");
+// Resident CTAs per SM the two-pass column kernels ask the register allocator for.
+#ifndef NTT_COLS2_MINB
+#define NTT_COLS2_MINB 4
+#endif
+#ifndef NTT_INV_COLS2_MINB
+#define NTT_INV_COLS2_MINB 4
+#endif
 
 template <class A, bool SIGNED>
-__global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant__ TransformArgs g) {
+__global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     release_dependents();
     constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
@@ -243,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_fwd_cols2(const __grid_constant
 }
 
 template <class A>
-__global__ void __launch_bounds__(kThreads, 4) k_inv_cols2(const __grid_constant__ TransformArgs g) {
+__global__ void __launch_bounds__(kThreads, NTT_INV_COLS2_MINB) k_inv_cols2(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
     const int prime = blockIdx.y;

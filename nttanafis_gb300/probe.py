@@ -10,7 +10,8 @@ _lib = None
 
 # Variant names of ntt_probe_arith, in order.
 VARIANTS = ["shoup32_butterfly", "montgomery32_butterfly", "shoup64_butterfly_50bit", "f64_fma_butterfly_50bit",
-            "imad", "imad_hi", "iadd3", "imul64", "dfma", "imad_wide", "i2f"]
+            "imad", "imad_hi", "iadd3", "imul64", "dfma", "imad_wide", "i2f",
+            "shoup32_wide_quotient_butterfly", "shoup32_c64_quotient_butterfly"]
 
 
 def library() -> ctypes.CDLL:
