@@ -308,6 +308,13 @@ uint8_t ntt_crt_pair_combine_device(uint64_t first, uint64_t second, int64_t* d_
  * synchronizes `stream` and allocates its operands for the call. Calls made by other
  * threads meanwhile may run with a split under trial (their results stay exact). No
  * reference counterpart: the reference fixes its geometry in Geometry::select. */
+/* Products of single calls (workspace and plan calls; batches keep the transforms)
+ * with a_len * b_len <= max_products limb products and at most 1,024 result limbs
+ * take the direct column-sum basecase: one thread-block cluster of 1 to 8 CTAs, no
+ * scratch. 0 turns it off. Process-wide; returns the previous threshold. It changes
+ * speed, never results. No reference counterpart: the reference's own basecase
+ * crossover is inside its planner. */
+uint64_t ntt_school_set(uint64_t max_products);
 int ntt_split_set(int log_t, int log_r);
 int ntt_split_get(int log_t);
 int ntt_split_range(int log_t, int* lo, int* hi);

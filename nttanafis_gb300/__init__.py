@@ -10,6 +10,7 @@ from .api import (  # noqa: F401
     Request,
     MulPlan,
     get_split,
+    set_basecase_limit,
     load_splits,
     save_splits,
     set_split,

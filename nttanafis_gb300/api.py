@@ -111,6 +111,7 @@ _SIGNATURES = [
     ("ntt_timing_stop", ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("ntt_lookback_timeouts", ctypes.c_uint32, []),
     ("ntt_debug_stall_lookback", ctypes.c_int, [ctypes.c_int]),
+    ("ntt_school_set", ctypes.c_uint64, [ctypes.c_uint64]),
     ("ntt_split_set", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     ("ntt_split_get", ctypes.c_int, [ctypes.c_int]),
     ("ntt_split_range", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
@@ -186,6 +187,12 @@ def debug_stall_lookback(count: int) -> int:
     """Test hook: the next `count` look-back CRT launches start with their tile
     counter at 1, so the bounded wait for tile 0 runs out. Returns the previous count."""
     return int(library().ntt_debug_stall_lookback(int(count)))
+
+
+def set_basecase_limit(max_products: int) -> int:
+    """Single-call products with a_len * b_len <= max_products take the direct
+    column-sum basecase (0: never); returns the previous limit."""
+    return int(library().ntt_school_set(int(max_products)))
 
 
 def split_range(log_t: int) -> Optional[tuple[int, int]]:

@@ -23,8 +23,8 @@ CSRC = HERE / "csrc"
 LIBDIR = HERE / "_lib"
 LIB = LIBDIR / "libntt_gb300.so"
 PROBE_LIB = LIBDIR / "libntt_probe.so"
-SOURCES = ["api.cu", "plan.cu", "exec.cu", "batch.cu", "transform.cu", "small.cu", "crt.cu", "noalloc.cu",
-           "field.cu"]
+SOURCES = ["api.cu", "plan.cu", "exec.cu", "batch.cu", "transform.cu", "small.cu", "crt.cu", "school.cu",
+           "noalloc.cu", "field.cu"]
 PROBE_SOURCES = ["probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -485,6 +485,8 @@ int ntt_split_set(int log_t, int log_r) {
     return prev ? prev : log_t / 2;
 }
 
+uint64_t ntt_school_set(uint64_t max_products) { return g_school_max.exchange(max_products); }
+
 int ntt_split_get(int log_t) {
     int lo = 0, hi = 0;
     if (!split_range(log_t, lo, hi)) return 0;

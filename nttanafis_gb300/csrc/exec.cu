@@ -102,9 +102,25 @@ static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_
 // Enqueues one product or convolution on `st`. With `b_ready` set (an event that
 // completes when operand b is in place), the column pass of a runs first and the
 // one of b waits for that event, so b's upload overlaps a's pass.
+std::atomic<uint64_t> g_school_max{kSchoolDefaultProducts};
+
+bool takes_basecase(const Geom& g) {
+    return !g.conv && !g.split() && (double)g.la * (double)g.lb <= (double)g_school_max.load() &&
+           school_fits(g.la, g.lb);
+}
+
 bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_dst,
              void* scratch, cudaStream_t st, cudaEvent_t b_ready, u32* status, bool admit) {
     mark(st);
+    if (takes_basecase(g)) {  // one cluster of direct column sums, no scratch
+        if (!kernels_ready()) return false;
+        if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
+        note_launches(1);
+        const bool ok = cuda_ok(launch_school_mul(d_a, g.la, square ? d_a : d_b, square ? g.la : g.lb, d_dst, st),
+                                "basecase launch");
+        mark(st);
+        return ok;
+    }
     if (g.split()) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         const bool ok = execute_split(g, d_a, square ? d_a : d_b, d_dst, scratch, st, status);

@@ -95,6 +95,9 @@ int single_log_r(const Geom& g);
 // first use), or with the split in use.
 bool prepare_params(const Geom& g, int log_r, PrimeSet& ps, CrtParams& cp);
 bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp);
+// The kernel attributes (shared-memory opt-in, cluster sizes) are set on the current
+// device; a lock-free check after the first call.
+bool kernels_ready();
 
 // ---------------------------------------------------------------------------------
 // Enqueue (exec.cu)
@@ -104,6 +107,11 @@ bool prepare_params(const Geom& g, PrimeSet& ps, CrtParams& cp);
 // status: the failure bytes of launch.h, or null.
 bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st,
                  u32* status = nullptr);
+// Products of single calls with at most this many limb products (a_len * b_len)
+// take the direct column-sum basecase (school.cu) when it holds them; 0 turns it
+// off. Set by ntt_school_set.
+extern std::atomic<uint64_t> g_school_max;
+bool takes_basecase(const Geom& g);
 // One product or convolution on `st`; b_ready (optional) completes when operand b
 // is in place. status: the failure bytes of launch.h, or null. admit: check a
 // convolution's coefficient bounds on the device first (device-pointer calls; the

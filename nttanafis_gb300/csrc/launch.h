@@ -182,6 +182,19 @@ cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cuda
 cudaError_t launch_split_descs(ProductDesc* d, u64 first, u64 count, const u64* a, u64 la, const u64* b, u64 lb,
                                u64 block, u64* dst, u64* odd, uint8_t* arena, u64 member_bytes, u64 spec_bytes,
                                cudaStream_t st);
+// Short products by direct column sums in one thread-block cluster (school.cu): for
+// products of at most kSchoolMaxOut limbs (one CRT tile); needs no scratch.
+constexpr int kSchoolSmemMax = 200 * 1024;
+// Default basecase threshold in limb products (a_len * b_len), from per-call timings
+// on GB300: the basecase wins up to 96 x 96 (6.2 against 8.2 us), ties at 128 x 128
+// (8.2 us each) and loses from 192 x 192 on (256 x 256: 10.3 against 8.2 us).
+constexpr u64 kSchoolDefaultProducts = 12288;
+constexpr u64 kSchoolMaxOut = kCrtTile;
+bool school_fits(u64 la, u64 lb);
+// Dynamic shared memory of the basecase with a cluster of cl CTAs.
+size_t school_smem_cl(u64 la, u64 lb, int cl);
+cudaError_t launch_school_mul(const u64* a, u64 la, const u64* b, u64 lb, u64* dst, cudaStream_t st);
+cudaError_t init_school_kernels();
 cudaError_t launch_conv_schoolbook(const u64* a, u64 la, const u64* b, u64 lb, u64* dst,
                                    int stride, bool sign, cudaStream_t st, const u32* votes = nullptr,
                                    u32* status = nullptr);

@@ -292,12 +292,24 @@ static bool upload(uint2** dst, const std::vector<uint2>& host) {
                    "cudaMemcpy(table)");
 }
 
+// Kernel attributes of every kernel on device `dev` (caller holds g_table_mutex).
+static std::atomic<bool> g_kernels_ready[64];
 static bool device_ready(int dev) {
     if (g_device_ready[dev]) return true;
     if (!cuda_ok(init_transform_kernels(), "kernel attributes")) return false;
     if (!cuda_ok(init_crt_kernels(), "kernel attributes")) return false;
+    if (!cuda_ok(init_school_kernels(), "kernel attributes")) return false;
     g_device_ready[dev] = true;
+    if (dev >= 0 && dev < 64) g_kernels_ready[dev].store(true, std::memory_order_release);
     return true;
+}
+
+bool kernels_ready() {
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
+    if (dev >= 0 && dev < 64 && g_kernels_ready[dev].load(std::memory_order_acquire)) return true;
+    std::lock_guard<std::mutex> lock(g_table_mutex);
+    return device_ready(dev);
 }
 
 static bool prime_tables(int dev, u32 p, PrimeTables& out) {

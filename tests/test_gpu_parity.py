@@ -41,6 +41,15 @@ def ws(gpu):
     w.close()
 
 
+@pytest.fixture
+def transforms_only(gpu):
+    """Short products through the transforms (the basecase off), so that the
+    one-CTA and fused transform kernels stay covered at every size."""
+    previous = gpu.set_basecase_limit(0)
+    yield
+    gpu.set_basecase_limit(previous)
+
+
 def gpu_mul(ws, a, b, extra=2):
     dst = np.full(a.size + b.size + extra, MASK, dtype=np.uint64)
     assert ws.mul(dst, a, b), "mul failed"
@@ -70,13 +79,29 @@ def test_golden_squares(ws, golden):
         assert np.array_equal(gpu_sqr(ws, a), hexlimbs(case["square"]))
 
 
-def test_config_1024_mul_and_sqr_match_oracle(ws):
-    a, b = operand(1024, 1), operand(1024, 2)
-    assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b))
-    assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a))
+@pytest.mark.parametrize("path", ["default", "transforms"])
+def test_config_1024_mul_and_sqr_match_oracle(ws, gpu, path):
+    previous = gpu.set_basecase_limit(0) if path == "transforms" else None
+    try:
+        a, b = operand(1024, 1), operand(1024, 2)
+        assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b))
+        assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a))
+    finally:
+        if previous is not None:
+            gpu.set_basecase_limit(previous)
 
 
-def test_small_shapes_every_length(ws):
+@pytest.mark.parametrize("path", ["default", "transforms"])
+def test_small_shapes_every_length(ws, gpu, path):
+    previous = gpu.set_basecase_limit(0) if path == "transforms" else None
+    try:
+        _small_shapes_every_length(ws)
+    finally:
+        if previous is not None:
+            gpu.set_basecase_limit(previous)
+
+
+def _small_shapes_every_length(ws):
     # proptest range of src/tests/products.rs:134-135: 1..=40 limbs each
     rng = np.random.default_rng(11)
     for la in range(1, 41):
@@ -98,7 +123,7 @@ def test_unbalanced_either_order(ws):
 
 
 @pytest.mark.parametrize("log_t", range(4, 14))
-def test_fused_cluster_every_size(ws, log_t):
+def test_fused_cluster_every_size(ws, transforms_only, log_t):
     # every single-product fused size (T = 2^4 .. 2^13): products that fill T,
     # squares, and all-ones operands whose carries run across every CRT tile
     half = 1 << (log_t - 1)
