@@ -14,7 +14,7 @@ namespace ntt {
 // primes, sign and square) whose descriptors sit in device memory; max_len is the
 // longest member output (limbs of a product, coefficients of a convolution).
 bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st,
-                 u32* status) {
+                 u32* status, u32* shared_spec) {
     TransformArgs ta;
     memset(&ta, 0, sizeof(ta));
     CrtParams cp;
@@ -22,6 +22,8 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
     if (!prepare_params(g0, log_r, ta.ps, cp)) return false;
     ta.batch = descs;
     ta.count = n;
+    ta.shared_spec = shared_spec;
+    ta.a_only = shared_spec ? 1 : 0;
     ta.np = g0.np;
     ta.log_t = g0.log_t;
     ta.wide = g0.wide;
@@ -35,7 +37,7 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
         if (!cuda_ok(launch_conv_admit_batch(descs, n, sign, st), "batched admission launch")) return false;
         mark(st);
     }
-    if (!g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
+    if (!shared_spec && !g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
         note_launches(1);
         const bool ok = cuda_ok(launch_small_fused(ta, cp, sq, st), "batched fused product launch");
         mark(st);
@@ -43,7 +45,9 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
     }
     if (g0.log_t <= kMaxBlockLog) {
         note_launches(1);
-        if (!cuda_ok(launch_small(ta, sq, sign, st), "batched transform launch")) return false;
+        if (!cuda_ok(launch_small(ta, shared_spec ? kRowPre : sq ? kRowSqr : kRowMul, sign, st),
+                     "batched transform launch"))
+            return false;
         mark(st);
     } else {
         ta.log_r = log_r;
@@ -51,7 +55,8 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
         note_launches(3);
         if (!cuda_ok(launch_fwd_cols(ta, sq, sign, st), "batched column pass launch")) return false;
         mark(st);
-        if (!cuda_ok(launch_rows(ta, sq, st), "batched row pass launch")) return false;
+        if (!cuda_ok(launch_rows(ta, shared_spec ? kRowPre : sq ? kRowSqr : kRowMul, st), "batched row pass launch"))
+            return false;
         mark(st);
         if (!cuda_ok(launch_inv_cols(ta, st), "batched inverse column pass launch")) return false;
         mark(st);
@@ -66,9 +71,11 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
     return ok;
 }
 
-// Enqueues a split product: the blocks of the longer operand times the shorter one
-// as batch members in chunks (the even blocks' products straight into dst, the odd
-// ones' into a second number), then dst += odd with carries.
+// Enqueues a split product: the spectrum of the shorter operand once (its column
+// pass, then the row pass in kRowFwd mode, or the one-CTA transform), then the
+// blocks of the longer operand as batch members in chunks, each transforming its
+// block alone and multiplying by that spectrum (the even blocks' products straight
+// into dst, the odd ones' into a second number), then dst += odd with carries.
 static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_dst, void* scratch, cudaStream_t st,
                           u32* status) {
     const bool swap = g.la < g.lb;
@@ -79,12 +86,40 @@ static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_
     ProductDesc* descs = (ProductDesc*)base;
     u64* odd = (u64*)(base + g.split_desc_bytes());
     u32* flags = (u32*)((uint8_t*)odd + g.split_odd_bytes());
-    uint8_t* arena = (uint8_t*)flags + g.split_flag_bytes();
-    const u64 member = g.member_bytes(false), spec = g.spec_bytes(false);
+    u32* spectrum = (u32*)((uint8_t*)flags + g.split_flag_bytes());
+    uint8_t* arena = (uint8_t*)spectrum + g.spec_bytes(true);
+    const u64 member = g.member_bytes(false), spec = g.spec_bytes(true);
     if (!cuda_ok(cudaMemsetAsync(d_dst, 0, g.out_len * 8, st), "zero product") ||
         !cuda_ok(cudaMemsetAsync(odd, 0, g.out_len * 8, st), "zero odd blocks") ||
         !cuda_ok(cudaMemsetAsync(flags, 0, carry_scratch_bytes(g.out_len), st), "zero carry flags"))
         return false;
+    // the shorter operand's spectrum, once for every block
+    TransformArgs tb;
+    memset(&tb, 0, sizeof(tb));
+    CrtParams cp;
+    const int log_r = four_step_log_r(g);
+    if (!prepare_params(g, log_r, tb.ps, cp)) return false;
+    tb.a = tb.b = sht;
+    tb.la = tb.lb = S;
+    tb.spec = spectrum;
+    tb.conv_len = g.block + S - 1;
+    tb.np = g.np;
+    tb.log_t = g.log_t;
+    tb.log_r = log_r;
+    tb.log_c = g.log_t - log_r;
+    tb.wide = g.wide;
+    tb.op_count = 1;
+    tb.shared_spec = spectrum;
+    if (log_r == 0) {  // one CTA per prime holds the block transform
+        note_launches(1);
+        if (!cuda_ok(launch_small(tb, kRowFwd, false, st), "spectrum transform launch")) return false;
+    } else {
+        note_launches(2);
+        if (!cuda_ok(launch_fwd_cols(tb, true, false, st), "spectrum column pass launch") ||
+            !cuda_ok(launch_rows(tb, kRowFwd, st), "spectrum row pass launch"))
+            return false;
+    }
+    mark(st);
     const u64 chunk = g.split_chunk();
     for (u64 first = 0; first < g.blocks; first += chunk) {
         const u64 count = std::min(chunk, g.blocks - first);
@@ -92,7 +127,7 @@ static bool execute_split(const Geom& g, const u64* d_a, const u64* d_b, u64* d_
         if (!cuda_ok(launch_split_descs(descs, first, count, lng, L, sht, S, g.block, d_dst, odd, arena, member, spec,
                                         st),
                      "split descriptors") ||
-            !run_members(descs, (int)count, g, false, g.block + S, st, status))
+            !run_members(descs, (int)count, g, false, g.block + S, st, status, spectrum))
             return false;
     }
     note_launches(1);
@@ -186,7 +221,7 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
         ta.max_a = g.max_a;
         ta.max_b = square ? g.max_a : g.max_b;
         note_launches(1);
-        if (!cuda_ok(launch_small(ta, square, sign, st), "transform launch")) return false;
+        if (!cuda_ok(launch_small(ta, square ? kRowSqr : kRowMul, sign, st), "transform launch")) return false;
         mark(st);
     } else {
         ta.log_r = log_r;
@@ -205,7 +240,7 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
         }
         note_launches(3);
         mark(st);
-        if (!cuda_ok(launch_rows(ta, square, st), "row pass launch")) return false;
+        if (!cuda_ok(launch_rows(ta, square ? kRowSqr : kRowMul, st), "row pass launch")) return false;
         mark(st);
         if (!cuda_ok(launch_inv_cols(ta, st), "inverse column pass launch")) return false;
         mark(st);

@@ -59,23 +59,27 @@ struct Geom {
     // residues (0 for a schoolbook convolution)
     u64 spec_bytes(bool square) const { return (spec_words(square) * 4 + 255) & ~(u64)255; }
     u64 tail_bytes(u64 out) const { return conv ? 0 : (carry_scratch_bytes(out) + 255) & ~(u64)255; }
-    // scratch of one product of this geometry (one block if split)
+    // scratch of one product of this geometry; for a split product, of one block,
+    // whose other factor is the stored spectrum of the shorter operand (one operand
+    // of residues)
     u64 member_bytes(bool square) const {
-        const u64 out = split() ? block + std::min(la, lb) : out_len;
-        return head_bytes() + spec_bytes(square) + tail_bytes(out);
+        if (split()) return spec_bytes(true) + tail_bytes(block + std::min(la, lb));
+        return head_bytes() + spec_bytes(square) + tail_bytes(out_len);
     }
     // blocks per enqueue of a split product: bounded launch grids and arena
     u64 split_chunk() const {
         const u64 by_bytes = std::max<u64>(1, ((u64)512 << 20) / member_bytes(false));
         return std::min<u64>({blocks, 16384, by_bytes});
     }
-    // split: [descriptors][odd-block sums (out_len limbs)][add flags][member arenas]
+    // split: [descriptors][odd-block sums (out_len limbs)][add flags][spectrum of the
+    // shorter operand][member arenas]
     u64 split_desc_bytes() const { return (split_chunk() * sizeof(ProductDesc) + 255) & ~(u64)255; }
     u64 split_odd_bytes() const { return (out_len * 8 + 255) & ~(u64)255; }
     u64 split_flag_bytes() const { return (carry_scratch_bytes(out_len) + 255) & ~(u64)255; }
     u64 scratch_bytes(bool square) const {
         if (split())
-            return split_desc_bytes() + split_odd_bytes() + split_flag_bytes() + split_chunk() * member_bytes(false);
+            return split_desc_bytes() + split_odd_bytes() + split_flag_bytes() + spec_bytes(true) +
+                   split_chunk() * member_bytes(false);
         return member_bytes(square);
     }
 };
@@ -104,9 +108,10 @@ bool kernels_ready();
 
 // The kernels of n batch members of one transform class, descriptors in device
 // memory; convolution members are admitted on the device (their votes).
-// status: the failure bytes of launch.h, or null.
+// status: the failure bytes of launch.h, or null. shared_spec: the stored spectrum
+// of a factor all members share (block-split products), or null.
 bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 max_len, cudaStream_t st,
-                 u32* status = nullptr);
+                 u32* status = nullptr, u32* shared_spec = nullptr);
 // Products of single calls with at most this many limb products (a_len * b_len)
 // take the direct column-sum basecase (school.cu) when it holds them; 0 turns it
 // off. Set by ntt_school_set.

@@ -91,7 +91,20 @@ struct TransformArgs {
     u32* votes;
     u64 max_a, max_b;
     int admit;         // batch: check the members' coefficients (their votes)
+    // A spectrum shared by the members (the shorter operand of a block-split
+    // product): [np][T] u32, written by the row pass in kRowFwd mode, read in
+    // kRowPre; a_only: the members' column passes transform operand a alone.
+    u32* shared_spec;
+    int a_only;
     PrimeSet ps;
+};
+
+// Transform modes of the row pass (k_rows) and the one-CTA transform (k_small).
+enum RowMode : int {
+    kRowMul = 0,  // a and b: forward both, pointwise a * b, inverse
+    kRowSqr = 1,  // a alone: forward, pointwise a * a, inverse
+    kRowFwd = 2,  // a alone: forward; its reduced spectrum written to shared_spec
+    kRowPre = 3,  // a alone: forward, pointwise by the spectrum in shared_spec, inverse
 };
 
 // Exact-CRT constants of one prime set (words in radix 2^32). The transforms fold
@@ -123,7 +136,7 @@ inline void fill_multiples(CrtParams& cp) {
 }
 
 // Launchers; each returns the launch status.
-cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
+cudaError_t launch_small(const TransformArgs& g, int mode, bool sign, cudaStream_t st);
 // Whole products of T <= 2^kFusedMaxLog points with kFusedPrimes primes in one
 // kernel: a cluster of one CTA per prime transforms, then reconstructs and carries
 // the product from the cluster's shared memory. Returns cudaErrorNotSupported for
@@ -131,7 +144,7 @@ cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStr
 constexpr int kFusedMaxLog = 13, kFusedPrimes = 5;
 cudaError_t launch_small_fused(const TransformArgs& g, const CrtParams& cp, bool square, cudaStream_t st);
 cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cudaStream_t st);
-cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st);
+cudaError_t launch_rows(const TransformArgs& g, int mode, cudaStream_t st);
 cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st);
 
 // Failure status of the calls of a workspace or batch: four bytes in page-locked

@@ -267,7 +267,7 @@ extern "C" uint8_t ntt_mul_noalloc_device(uint64_t* d_dst, size_t dst_len, const
         pp.inv = pp.fwd + kNaPoints;
         ta.ps.pr[i] = pp;
     }
-    cudaError_t e = launch_small(ta, square, false, st);
+    cudaError_t e = launch_small(ta, square ? kRowSqr : kRowMul, false, st);
     if (e == cudaSuccess)
         e = launch_crt_mul(d->scratch, log_t, conv_len, out_len, d_dst, (uint8_t*)(d->scratch + kNaSpecWords),
                            g_na_crt, st);

@@ -142,19 +142,30 @@ constexpr u64 kMaxSplitLimbs = (u64)1 << 40;
 // Block split of an unbalanced product (the reference's Geometry::cheapest_blocks,
 // src/profile/planner.rs:291-393, restated for this library's transforms): the
 // longer operand (L limbs) in blocks of B = 2^k - S + 1 limbs, each multiplied by
-// the shorter one (S limbs) with 2^k-point transforms. Cost in butterfly levels:
-// three transforms per block, n * 3 * 2^k * k, against 3 * 2^K * K for one
-// transform of the whole product. Returns the chosen k, or 0 when one transform
-// is cheaper (by the margin that pays for the block sums and the final addition).
+// the shorter one (S limbs) with 2^k-point transforms. The shorter operand's
+// spectrum is computed once and shared by every block (the reference's shared
+// short-operand spectrum, src/multiply/execute.rs:114-130). Cost in butterfly
+// levels: two transforms per block and one for the shorter operand,
+// (2n + 1) * 2^k * k, plus a fixed kSplitOverhead for the block sums, the final
+// addition and about ten more launches and copies, against 3 * 2^K * K for one
+// transform of the whole product. Returns the chosen k, or 0 when one transform is
+// within the margin. Measured on GB300 (per call, split against one transform):
+// 1,048,576 x 1,024 99 against 160 us, 4,194,304 x 524,288 477 against 797 us,
+// 1,048,576 x 131,072 149 against 165 us; below, the fixed part dominates
+// (20,000 x 300: 41 against 24 us; 16,384 x 4,096: 51 against 24 us).
+#ifndef NTT_SPLIT_MARGIN
+#define NTT_SPLIT_MARGIN 0.8
+#endif
+constexpr double kSplitOverhead = 16777216.0;  // butterfly levels, about 25 us on GB300
 static int split_log(u64 L, u64 S, int full_log) {
     const double full = full_log <= kMaxLogT ? 3.0 * std::ldexp(1.0, full_log) * full_log : 1e300;
     int best_k = 0;
-    double best = 0.8 * full;
+    double best = NTT_SPLIT_MARGIN * full;
     const int lo = std::max(kSmallSplitLog, ceil_log2(2 * S));
     for (int k = lo; k <= kMaxLogT && k < full_log; ++k) {
         const u64 B = ((u64)1 << k) - S + 1;
         const double n = (double)((L + B - 1) / B);
-        const double cost = n * 3.0 * std::ldexp(1.0, k) * k;
+        const double cost = (2.0 * n + 1.0) * std::ldexp(1.0, k) * k + kSplitOverhead;
         if (cost < best) {
             best = cost;
             best_k = k;

@@ -19,9 +19,12 @@ namespace ntt {
 
 // One CTA transforms one prime: pack, forward a (and b), pointwise, inverse, scale.
 // grid = (np, members). The prime-0 CTA of a member also clears its CRT flags.
-template <class A, bool SQUARE, bool SIGNED, int LOG_N>
+// MODE (RowMode, launch.h): kRowMul a * b, kRowSqr a * a, kRowFwd the forward
+// spectrum of a written to g.shared_spec, kRowPre a times the spectrum there.
+template <class A, int MODE, bool SIGNED, int LOG_N>
 __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
+    constexpr bool SQUARE = MODE != kRowMul;
     constexpr int N = 1 << LOG_N;
     constexpr int VS = padded_len(N);
     const PrimeParams& pp = g.ps.pr[blockIdx.x];
@@ -54,10 +57,15 @@ __global__ void __launch_bounds__(kThreads) k_small(const __grid_constant__ Tran
     if (check)  // every vote is written: vote 0 carries the verdict
         for (int i = threadIdx.x; i < kAdmitSlots; i += kThreads) votes[i] = i == 0 && bad ? 1u : 0u;
     dif_full<A, LOG_N, kThreads, SQUARE ? 1 : 2, VS>(sm, pp.fwd, pp.p);
+    u32* spectrum = g.shared_spec + ((size_t)blockIdx.x << LOG_N);
+    if constexpr (MODE == kRowFwd) {
+        for (int i = threadIdx.x; i < N; i += kThreads) spectrum[i] = sa[pad_index(i)];
+        return;
+    }
     for (int i = threadIdx.x; i < N; i += kThreads) {
         const int k = pad_index(i);
         const u32 x = sa[k];
-        const u32 y = SQUARE ? x : sb[k];
+        const u32 y = MODE == kRowMul ? sb[k] : MODE == kRowPre ? __ldg(spectrum + i) : x;
         sa[k] = A::mulc(A::pointwise(x, y, pp.p, pp.pni), pp.scale, pp.p);
     }
     __syncthreads();
@@ -172,11 +180,13 @@ __global__ void __launch_bounds__(kThreads) k_small_fused(const __grid_constant_
 // ---------------------------------------------------------------------------------
 
 template <class A, int L>
-static cudaError_t small_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
-    auto k = square ? (sign ? k_small<A, true, true, L> : k_small<A, true, false, L>)
-                    : (sign ? k_small<A, false, true, L> : k_small<A, false, false, L>);
+static cudaError_t small_at(const TransformArgs& g, int mode, bool sign, cudaStream_t st, bool init) {
+    auto k = mode == kRowMul ? (sign ? k_small<A, kRowMul, true, L> : k_small<A, kRowMul, false, L>)
+             : mode == kRowSqr ? (sign ? k_small<A, kRowSqr, true, L> : k_small<A, kRowSqr, false, L>)
+             : mode == kRowFwd ? k_small<A, kRowFwd, false, L>
+                               : k_small<A, kRowPre, false, L>;
     if (init) return opt_in(k);
-    const size_t smem = (size_t)(square ? 1 : 2) * padded_len(1 << L) * sizeof(u32);
+    const size_t smem = (size_t)(mode == kRowMul ? 2 : 1) * padded_len(1 << L) * sizeof(u32);
     k<<<dim3(g.np, g.batch ? g.count : 1), kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
@@ -216,18 +226,18 @@ static cudaError_t fused_any(const TransformArgs& g, const CrtParams* cp, bool s
     }
 }
 
-static cudaError_t small_any(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
+static cudaError_t small_any(const TransformArgs& g, int mode, bool sign, cudaStream_t st, bool init) {
     switch (g.log_t) {
-        case 4: return small_at<LazyArith, 4>(g, square, sign, st, init);
-        case 5: return small_at<LazyArith, 5>(g, square, sign, st, init);
-        case 6: return small_at<LazyArith, 6>(g, square, sign, st, init);
-        case 7: return small_at<LazyArith, 7>(g, square, sign, st, init);
-        case 8: return small_at<LazyArith, 8>(g, square, sign, st, init);
-        case 9: return small_at<LazyArith, 9>(g, square, sign, st, init);
-        case 10: return small_at<LazyArith, 10>(g, square, sign, st, init);
-        case 11: return small_at<LazyArith, 11>(g, square, sign, st, init);
-        case 12: return small_at<LazyArith, 12>(g, square, sign, st, init);
-        case 13: return small_at<LazyArith, 13>(g, square, sign, st, init);
+        case 4: return small_at<LazyArith, 4>(g, mode, sign, st, init);
+        case 5: return small_at<LazyArith, 5>(g, mode, sign, st, init);
+        case 6: return small_at<LazyArith, 6>(g, mode, sign, st, init);
+        case 7: return small_at<LazyArith, 7>(g, mode, sign, st, init);
+        case 8: return small_at<LazyArith, 8>(g, mode, sign, st, init);
+        case 9: return small_at<LazyArith, 9>(g, mode, sign, st, init);
+        case 10: return small_at<LazyArith, 10>(g, mode, sign, st, init);
+        case 11: return small_at<LazyArith, 11>(g, mode, sign, st, init);
+        case 12: return small_at<LazyArith, 12>(g, mode, sign, st, init);
+        case 13: return small_at<LazyArith, 13>(g, mode, sign, st, init);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -238,8 +248,8 @@ cudaError_t launch_small_fused(const TransformArgs& g, const CrtParams& cp, bool
     return fused_any(g, &cp, square, st, false);
 }
 
-cudaError_t launch_small(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
-    return small_any(g, square, sign, st, false);
+cudaError_t launch_small(const TransformArgs& g, int mode, bool sign, cudaStream_t st) {
+    return small_any(g, mode, sign, st, false);
 }
 
 // Raises the dynamic shared-memory limit of every one-CTA transform kernel.
@@ -249,8 +259,9 @@ cudaError_t init_small_kernels() {
     for (int sq = 0; sq < 2; ++sq)
         for (int l = 4; l <= kMaxBlockLog && e == cudaSuccess; ++l) {
             g.log_t = l;
-            e = small_any(g, sq, false, 0, true);
-            if (e == cudaSuccess) e = small_any(g, sq, true, 0, true);
+            e = small_any(g, sq ? kRowSqr : kRowMul, false, 0, true);
+            if (e == cudaSuccess) e = small_any(g, sq ? kRowSqr : kRowMul, true, 0, true);
+            if (e == cudaSuccess) e = small_any(g, sq ? kRowFwd : kRowPre, false, 0, true);
             if (e == cudaSuccess && l <= kFusedMaxLog) e = fused_any(g, nullptr, sq, 0, true);
         }
     return e;

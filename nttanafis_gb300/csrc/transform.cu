@@ -87,9 +87,10 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;  // sweeps per batch; B*RS is a multiple of 32
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
     const int prime = blockIdx.y;
-    // grid.z: operands (1 or 2) of one member, or 2 per member in a batch
-    const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z + g.op_base;
-    const Member m = member_of(g, g.batch ? (blockIdx.z >> 1) : 0, false);
+    // grid.z: operands (1 or 2) of one member, or per member in a batch (2, or 1
+    // when the batch's other factor is a stored spectrum)
+    const int op = g.batch ? (g.a_only ? 0 : blockIdx.z & 1) : blockIdx.z + g.op_base;
+    const Member m = member_of(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, false);
     if (op && m.square) return;
     const PrimeParams& pp = g.ps.pr[prime];
     const u64* __restrict__ src = op ? m.b : m.a;
@@ -193,8 +194,8 @@ __global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __
     release_dependents();
     constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
     const int prime = blockIdx.y;
-    const int op = g.batch ? (blockIdx.z & 1) : blockIdx.z + g.op_base;
-    const Member m = member_of(g, g.batch ? (blockIdx.z >> 1) : 0, false);
+    const int op = g.batch ? (g.a_only ? 0 : blockIdx.z & 1) : blockIdx.z + g.op_base;
+    const Member m = member_of(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, false);
     if (op && m.square) return;
     const PrimeParams& pp = g.ps.pr[prime];
     const u64* __restrict__ src = op ? m.b : m.a;
@@ -304,13 +305,13 @@ __host__ __device__ constexpr int row_log_rpc(int log_c) {
 // pointwise product and the first inverse pass run on the same registers (both
 // work on blocks of 2^RBL consecutive points), and the last inverse pass applies
 // the twiddle and writes global memory.
-template <class A, bool SQUARE, int LOG_C>
+template <class A, int MODE, int LOG_C>
 __global__ void __launch_bounds__(row_threads(LOG_C)) k_rows(const __grid_constant__ TransformArgs g) {
     constexpr int kRowThreads = row_threads(LOG_C);
     extern __shared__ u32 sm[];
     constexpr int C = 1 << LOG_C;
     constexpr int VS = padded_len(C);
-    constexpr int NV = SQUARE ? 1 : 2;           // a (and b), transformed together
+    constexpr int NV = MODE == kRowMul ? 2 : 1;  // a (and b), transformed together
     constexpr int LOG_RPC = row_log_rpc(LOG_C);
     constexpr int RPC = 1 << LOG_RPC;
     constexpr int RB = kMaxRB;
@@ -321,14 +322,16 @@ __global__ void __launch_bounds__(row_threads(LOG_C)) k_rows(const __grid_consta
     const int prime = blockIdx.y;
     const int row0 = blockIdx.x << LOG_RPC;
     const PrimeParams& pp = g.ps.pr[prime];
-    const Member m = member_of(g, blockIdx.z, SQUARE);
+    const Member m = member_of(g, blockIdx.z, NV == 1);
     release_dependents();
     u32* ra = m.spec + ((size_t)prime << g.log_t) + ((size_t)row0 << LOG_C);
     const u32* rb = m.spec + ((size_t)(g.np + prime) << g.log_t) + ((size_t)row0 << LOG_C);
+    // the stored spectrum of the rows (kRowFwd writes it, kRowPre multiplies by it)
+    u32* rs = g.shared_spec + ((size_t)prime << g.log_t) + ((size_t)row0 << LOG_C);
     // The rows' inverse four-step factors: RPC x 64 low-digit entries, RPC x C/64 high.
     uint2* il = reinterpret_cast<uint2*>(sm + RPC * NV * VS);
     uint2* ih = il + RPC * NL;
-    {
+    if constexpr (MODE != kRowFwd) {
         const uint2* lo = pp.i4_lo + (size_t)row0 * NL;
         const uint2* hi = pp.i4_hi + (size_t)row0 * NH;
         for (int i = threadIdx.x; i < RPC * (NL + NH); i += kRowThreads)
@@ -373,24 +376,41 @@ __global__ void __launch_bounds__(row_threads(LOG_C)) k_rows(const __grid_consta
 #pragma unroll
                 for (int k = 0; k < E; ++k) x[q][k] = base[q * VS + k];
             // a's last level stays open (the Montgomery product takes one factor
-            // below 4p), b's is reduced; the product is below 3p, so the first
-            // inverse level (twiddle 1) needs no products either
-            if constexpr (NV == 2) {
+            // below 4p), the other factor's is reduced; the product is below 3p, so
+            // the first inverse level (twiddle 1) needs no products either
+            u32 y[E];
+            if constexpr (MODE == kRowMul) {
                 u32(&xa)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
                 u32(&xb)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[1]);
                 dif_levels<A, RBL, 1, 1, false, true>(xa, pp.small_fwd, pp.p);
                 dif_levels<A, RBL, 1, 1>(xb, pp.small_fwd, pp.p);
-            } else {
-                dif_levels<A, RBL, 1, NV>(x, pp.small_fwd, pp.p);
+#pragma unroll
+                for (int k = 0; k < E; ++k) y[k] = x[1][k];
+            } else if constexpr (MODE == kRowSqr || MODE == kRowFwd) {
+                dif_levels<A, RBL, 1, 1>(x, pp.small_fwd, pp.p);
+                if constexpr (MODE == kRowFwd) {  // the reduced spectrum, stored
+                    u32* out = rs + ((size_t)r << LOG_C) + (gg << RBL);
+#pragma unroll
+                    for (int k = 0; k < E; ++k) out[k] = x[0][k];
+                    continue;
+                }
+#pragma unroll
+                for (int k = 0; k < E; ++k) y[k] = x[0][k];
+            } else {  // kRowPre: the other factor is the stored spectrum
+                const u32* in = rs + ((size_t)r << LOG_C) + (gg << RBL);
+#pragma unroll
+                for (int k = 0; k < E; ++k) y[k] = __ldg(in + k);
+                dif_levels<A, RBL, 1, 1, false, true>(x, pp.small_fwd, pp.p);
             }
 #pragma unroll
-            for (int k = 0; k < E; ++k) x[0][k] = A::pointwise(x[0][k], x[NV - 1][k], pp.p, pp.pni);
-            u32(&y)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
-            dit_levels<A, RBL, 1, 1, 1>(y, pp.small_inv, pp.p);
+            for (int k = 0; k < E; ++k) x[0][k] = A::pointwise(x[0][k], y[k], pp.p, pp.pni);
+            u32(&z)[1][E] = *reinterpret_cast<u32(*)[1][E]>(&x[0]);
+            dit_levels<A, RBL, 1, 1, 1>(z, pp.small_inv, pp.p);
 #pragma unroll
             for (int k = 0; k < E; ++k) base[k] = x[0][k];
         }
     }
+    if constexpr (MODE == kRowFwd) return;
     __syncthreads();
     dit_range<A, LOG_C, kRowThreads, RPC, NV * VS, RBL, LOG_C - RB>(sm, pp.inv, pp.p);
     // Last inverse pass: shared -> global, times the inverse four-step twiddle of
@@ -551,9 +571,9 @@ static size_t col_smem(int log_r, bool fwd) {
 }
 
 // Row residues (one or two vectors per row) plus the rows' inverse four-step factors.
-static size_t row_smem(int log_c, bool square) {
+static size_t row_smem(int log_c, int mode) {
     const size_t rpc = (size_t)1 << row_log_rpc(log_c);
-    return rpc * ((size_t)(square ? 1 : 2) * padded_len(1 << log_c) * sizeof(u32) +
+    return rpc * ((size_t)(mode == kRowMul ? 2 : 1) * padded_len(1 << log_c) * sizeof(u32) +
                   8 * (((size_t)1 << kRowTwLoBits) + ((size_t)1 << (log_c - kRowTwLoBits))));
 }
 
@@ -575,7 +595,7 @@ static size_t col2_smem(bool fwd) {
 template <class A, int L>
 static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     const unsigned ops = g.op_count ? g.op_count : (square ? 1 : 2);
-    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? 2 * g.count : ops);
+    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? (g.a_only ? 1 : 2) * g.count : ops);
     if constexpr (L == kCol2LogR) {
         auto k = sign ? k_fwd_cols2<A, true> : k_fwd_cols2<A, false>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
@@ -589,11 +609,14 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
 }
 
 template <class A, int L>
-static cudaError_t rows_at(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
-    auto k = square ? k_rows<A, true, L> : k_rows<A, false, L>;
+static cudaError_t rows_at(const TransformArgs& g, int mode, cudaStream_t st, bool init) {
+    auto k = mode == kRowMul ? k_rows<A, kRowMul, L>
+             : mode == kRowSqr ? k_rows<A, kRowSqr, L>
+             : mode == kRowFwd ? k_rows<A, kRowFwd, L>
+                               : k_rows<A, kRowPre, L>;
     if (init) return opt_in(k, NTT_ROWS_CARVEOUT);
     const dim3 grid(1u << (g.log_r - row_log_rpc(L)), g.np, g.batch ? g.count : 1);
-    const size_t smem = row_smem(L, square);
+    const size_t smem = row_smem(L, mode);
     return launch_dependent(k, grid, dim3(row_threads(L)), smem, st, g);
 }
 
@@ -627,20 +650,20 @@ static cudaError_t fwd_cols_any(const TransformArgs& g, bool square, bool sign, 
     }
 }
 
-static cudaError_t rows_any(const TransformArgs& g, bool square, cudaStream_t st, bool init) {
+static cudaError_t rows_any(const TransformArgs& g, int mode, cudaStream_t st, bool init) {
     if (g.wide) {
-        if (g.log_c == 12) return rows_at<WideArith, 12>(g, square, st, init);
-        if (g.log_c == 13) return rows_at<WideArith, 13>(g, square, st, init);
+        if (g.log_c == 12) return rows_at<WideArith, 12>(g, mode, st, init);
+        if (g.log_c == 13) return rows_at<WideArith, 13>(g, mode, st, init);
         return cudaErrorInvalidValue;
     }
     switch (g.log_c) {
-        case 7: return rows_at<LazyArith, 7>(g, square, st, init);
-        case 8: return rows_at<LazyArith, 8>(g, square, st, init);
-        case 9: return rows_at<LazyArith, 9>(g, square, st, init);
-        case 10: return rows_at<LazyArith, 10>(g, square, st, init);
-        case 11: return rows_at<LazyArith, 11>(g, square, st, init);
-        case 12: return rows_at<LazyArith, 12>(g, square, st, init);
-        case 13: return rows_at<LazyArith, 13>(g, square, st, init);
+        case 7: return rows_at<LazyArith, 7>(g, mode, st, init);
+        case 8: return rows_at<LazyArith, 8>(g, mode, st, init);
+        case 9: return rows_at<LazyArith, 9>(g, mode, st, init);
+        case 10: return rows_at<LazyArith, 10>(g, mode, st, init);
+        case 11: return rows_at<LazyArith, 11>(g, mode, st, init);
+        case 12: return rows_at<LazyArith, 12>(g, mode, st, init);
+        case 13: return rows_at<LazyArith, 13>(g, mode, st, init);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -664,9 +687,7 @@ static cudaError_t inv_cols_any(const TransformArgs& g, cudaStream_t st, bool in
 cudaError_t launch_fwd_cols(const TransformArgs& g, bool square, bool sign, cudaStream_t st) {
     return fwd_cols_any(g, square, sign, st, false);
 }
-cudaError_t launch_rows(const TransformArgs& g, bool square, cudaStream_t st) {
-    return rows_any(g, square, st, false);
-}
+cudaError_t launch_rows(const TransformArgs& g, int mode, cudaStream_t st) { return rows_any(g, mode, st, false); }
 cudaError_t launch_inv_cols(const TransformArgs& g, cudaStream_t st) { return inv_cols_any(g, st, false); }
 
 // Raises the dynamic shared-memory limit of every instantiation (both operand
@@ -684,7 +705,8 @@ cudaError_t init_transform_kernels() {
                     const bool col_ok = w ? l == 12 : l <= 11;
                     const bool row_ok = w ? l >= 12 : l >= 7;
                     if (col_ok) e = fwd_cols_any(g, sq, sg, 0, true);
-                    if (e == cudaSuccess && row_ok) e = rows_any(g, sq, 0, true);
+                    for (int mode = 0; mode < 4 && e == cudaSuccess && row_ok && sg == 0 && sq == 0; ++mode)
+                        e = rows_any(g, mode, 0, true);
                     if (e == cudaSuccess && col_ok) e = inv_cols_any(g, 0, true);
                 }
             }

@@ -256,9 +256,10 @@ def test_butterfly_probe_and_launch_counter(gpu):
     import torch
 
     ws = gpu.GpuMulWorkspace()
-    a = torch.from_numpy(operand(5000, 1).view(np.int64)).cuda()
-    b = torch.from_numpy(operand(4000, 2).view(np.int64)).cuda()
-    dst = torch.empty(9000, dtype=torch.int64, device="cuda")
+    a = torch.from_numpy(operand(6000, 1).view(np.int64)).cuda()
+    b = torch.from_numpy(operand(6000, 2).view(np.int64)).cuda()
+    assert gpu.MulPlan.new(6000, 6000).blocks == 0
+    dst = torch.empty(12000, dtype=torch.int64, device="cuda")
     assert ws.mul_device(dst, a, b)
     before = gpu.kernel_launches()
     assert ws.mul_device(dst, a, b)

@@ -301,10 +301,12 @@ def test_device_and_plan_scratch_paths(gpu):
     w.close()
 
 
-@pytest.mark.parametrize("la,lb", [(65536, 1024), (1024, 65536), (200000, 3001), (20000, 300), (1 << 20, 1024),
-                                   (1 << 20, 131072)])
+@pytest.mark.parametrize("la,lb", [(1 << 20, 1024), (1024, 1 << 20), (1 << 20, 3001), (600000, 1000), (1 << 20, 300),
+                                   (524288, 512), (1 << 20, 131072)])
 def test_block_split_matches_oracle(ws, gpu, la, lb):
-    # the longer operand in blocks times the shorter one, block sums added with carries
+    # the longer operand in blocks times the shorter one, whose spectrum every block
+    # shares (one-CTA block transforms at 2^11..2^13, four-step ones from 2^15),
+    # block sums added with carries
     assert gpu.MulPlan.new(la, lb).blocks > 1
     a, b = operand(la, 51), operand(lb, 52)
     assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b, THREADS)), (la, lb)
@@ -312,7 +314,7 @@ def test_block_split_matches_oracle(ws, gpu, la, lb):
 
 def test_block_split_all_ones(ws, gpu):
     # every block sum carries through the whole odd-block addition
-    for la, lb in [(65536, 1000), (70001, 1500)]:
+    for la, lb in [(1 << 20, 1000), ((1 << 20) + 7, 1500)]:
         assert gpu.MulPlan.new(la, lb).blocks > 1
         a = np.full(la, MASK, dtype=np.uint64)
         b = np.full(lb, MASK, dtype=np.uint64)
@@ -331,7 +333,7 @@ def test_block_split_beyond_one_transform(ws, gpu):
 def test_block_split_plan_scratch(gpu):
     import torch
 
-    la, lb = 90000, 2000
+    la, lb = 1 << 20, 2000
     plan = gpu.MulPlan.new(la, lb)
     assert plan.blocks > 1
     a, b = operand(la, 71), operand(lb, 72)
@@ -419,7 +421,7 @@ def test_poisoned_scratch_and_any_shape_order(gpu):
     # workspace serving fused, four-step and split shapes in a shuffled order
     import torch
 
-    shapes = [(3000, 2000), (70000, 50000), (90000, 2000), (1024, 1024), (5, 7), (1 << 17, 1 << 17), (40000, 300)]
+    shapes = [(3000, 2000), (70000, 50000), (600000, 1000), (1024, 1024), (5, 7), (1 << 17, 1 << 17), (40000, 300)]
     expected = {s: oracle.mul(operand(s[0], 121), operand(s[1], 122), THREADS) for s in shapes}
     stream = torch.cuda.current_stream()
     for la, lb in shapes:
