@@ -30,6 +30,8 @@ def lib() -> ctypes.CDLL:
         l.oracle_capacity.argtypes = [i32]
         l.oracle_schoolbook.argtypes = [vp, vp, u64, vp, u64]
         l.oracle_operand.argtypes = [vp, u64, u64]
+        l.oracle_transform_check.argtypes = [i32, i32, u64]
+        l.oracle_transform_check.restype = i32
         for name in ("oracle_mul", "oracle_sqr", "oracle_conv", "oracle_mul_plan", "oracle_conv_plan",
                      "oracle_row_shape", "oracle_capacity"):
             getattr(l, name).restype = i32
@@ -103,6 +105,11 @@ def schoolbook(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     out = np.zeros(a.size + b.size, dtype=np.uint64)
     lib().oracle_schoolbook(_p(out), _p(a), a.size, _p(b), b.size)
     return out
+
+
+def transform_check(prime: int, log_n: int, seed: int = 1) -> bool:
+    """The cache-blocked transforms equal the radix-2 ones bit for bit."""
+    return lib().oracle_transform_check(prime, log_n, seed) == 1
 
 
 def operand(length: int, seed: int) -> np.ndarray:

@@ -147,8 +147,10 @@ static const Cofactors* cof_of(int count) {
 int oracle_capacity(int count) { return count >= 1 && count <= MAX_PRIMES ? cof_of(count)->capacity : -1; }
 
 /* Cofactors::bounded (src/limb/cofactor.rs:59-111): residues already weighted by
- * the inverses; writes ceil(capacity/64) words of X. */
-static void cof_bounded(const Cofactors* t, int count, const u64* residue, u64* value) {
+ * the inverses; writes ceil(capacity/64) words of X. Instantiated per prime count
+ * (cof_bounded below) so that the word loops unroll. */
+static inline __attribute__((always_inline)) void cof_bounded_n(const Cofactors* t, const int count,
+                                                                const u64* residue, u64* value) {
     const int words = (t->capacity + 63) / 64;
     const int factor_words = count == 1 ? 1 : (MODULUS_BITS * (count - 1) + 63) / 64;
     u128 carry = 0;
@@ -169,6 +171,15 @@ static void cof_bounded(const Cofactors* t, int count, const u64* residue, u64* 
         const u64 d = v - m - borrow;
         borrow = (v < m) || (v - m < borrow);
         value[w] = d;
+    }
+}
+static void cof_bounded(const Cofactors* t, int count, const u64* residue, u64* value) {
+    switch (count) {
+#define COUNT_CASE(c) \
+    case c: cof_bounded_n(t, c, residue, value); break;
+        COUNT_CASE(1) COUNT_CASE(2) COUNT_CASE(3) COUNT_CASE(4) COUNT_CASE(5) COUNT_CASE(6) COUNT_CASE(7)
+        COUNT_CASE(8)
+#undef COUNT_CASE
     }
 }
 
@@ -431,16 +442,22 @@ static inline double submod(double a, double b, double p) {
 typedef struct {
     double p, pinv;
     u64 pi;
-    double* tw;  /* w^j, j < n/2, forward */
+    double* tw;  /* w^j, j < n/2, forward (radix-2 transforms only) */
     double* itw; /* w^-j */
     u64 n;
+    int prime;
 } Field;
 
-static int field_init(Field* f, int prime, u64 n) {
+/* tables: also build the radix-2 transforms' twiddles (the cache-blocked ones keep
+ * their own, retained across calls). */
+static int field_init(Field* f, int prime, u64 n, int tables) {
     f->pi = CAT_P[prime];
     f->p = (double)f->pi;
     f->pinv = 1.0 / f->p;
     f->n = n;
+    f->prime = prime;
+    f->tw = f->itw = NULL;
+    if (!tables) return 1;
     const u64 half = n / 2 ? n / 2 : 1;
     f->tw = (double*)malloc(half * sizeof(double));
     f->itw = (double*)malloc(half * sizeof(double));
@@ -496,6 +513,332 @@ static void ntt_inverse(double* a, const Field* f) {
     }
 }
 
+/* ------------------------------------------------------------------------------
+ * Cache-blocked transforms (the timed CPU path; src/transform/forward.rs:95-298,
+ * src/transform/inverse.rs:52-218 restated): the same cyclic DIF / DIT as
+ * ntt_forward / ntt_inverse above, depth first so that every sub-transform of up
+ * to 2^BLOCK_LOG points runs in cache, two levels per pass over memory above that,
+ * twiddles from per-level contiguous tables retained across calls (the reference's
+ * workspaces retain theirs, src/transform/twiddle.rs:50), and branch-free centred
+ * residues: every stored value lies in (-1.5p, 1.5p); sums are reduced by the
+ * nearest multiple of p, products by the exact FMA remainder without the final
+ * corrections (src/arch/scalar/product.rs:95-109). The output is canonicalised, so
+ * it equals the radix-2 transforms' bit for bit (oracle_transform_check). */
+#define BLOCK_LOG 12
+
+static inline double reduce_c(double v, double p, double pinv) { return fma(-nearest(v * pinv), p, v); }
+static inline double mul_c(double a, double b, double p, double pinv) {
+    const double h = a * b;
+    const double l = fma(a, b, -h);
+    const double q = nearest(h * pinv);
+    return fma(-q, p, h) + l;
+}
+static inline double canon_c(double v, double p) {
+    v = v < 0.0 ? v + p : v;
+    v = v < 0.0 ? v + p : v;
+    v = v >= p ? v - p : v;
+    return v >= p ? v - p : v;
+}
+
+/* Level-major centred roots of one prime and transform length, retained: L[h + j]
+ * = w_{2h}^j and IL[h + j] = w_{2h}^-j for h = 1, 2, ..., n/2 and j < h. Up to
+ * TABLE_BUDGET bytes are kept across calls; beyond that a call builds private
+ * tables and frees them (level_tables_release). */
+typedef struct {
+    u64 pi;
+    int log_n;
+    int cached;
+    double* fwd;
+    double* inv;
+} LevelTables;
+
+#define MAX_TABLES 64
+#define TABLE_BUDGET ((u64)1 << 31)
+static LevelTables TABLES[MAX_TABLES];
+static int TABLE_COUNT = 0;
+static u64 TABLE_BYTES = 0;
+static pthread_mutex_t TABLE_LOCK = PTHREAD_MUTEX_INITIALIZER;
+
+static int build_tables(LevelTables* t, int prime, int log_n) {
+    const u64 pi = CAT_P[prime], n = 1ull << log_n;
+    t->pi = pi;
+    t->log_n = log_n;
+    t->fwd = (double*)malloc(n * sizeof(double));
+    t->inv = (double*)malloc(n * sizeof(double));
+    u64* top = (u64*)malloc((n / 2 + 1) * sizeof(u64));
+    u64* itop = (u64*)malloc((n / 2 + 1) * sizeof(u64));
+    const int ok = t->fwd && t->inv && top && itop;
+    if (ok) {
+        const u64 w = powmod_int(CAT_G[prime], (pi - 1) / n, pi);
+        const u64 iw = powmod_int(w, pi - 2, pi);
+        u64 x = 1, ix = 1;
+        for (u64 j = 0; j < n / 2; ++j) {
+            top[j] = x;
+            itop[j] = ix;
+            x = mulmod_int(x, w, pi);
+            ix = mulmod_int(ix, iw, pi);
+        }
+        const double pd = (double)pi;
+        t->fwd[0] = t->inv[0] = 1.0;
+        for (u64 h = 1; h < n; h <<= 1)
+            for (u64 j = 0; j < h; ++j) {
+                const u64 a = top[j * (n / (2 * h))], b = itop[j * (n / (2 * h))];
+                t->fwd[h + j] = a > pi / 2 ? (double)a - pd : (double)a;
+                t->inv[h + j] = b > pi / 2 ? (double)b - pd : (double)b;
+            }
+    } else {
+        free(t->fwd);
+        free(t->inv);
+        t->fwd = t->inv = NULL;
+    }
+    free(top);
+    free(itop);
+    return ok;
+}
+
+/* Tables of (prime, 2^log_n) in *out: the retained copy, or private ones. */
+static int level_tables(int prime, int log_n, LevelTables* out) {
+    const u64 pi = CAT_P[prime], bytes = (2ull << log_n) * sizeof(double);
+    pthread_mutex_lock(&TABLE_LOCK);
+    for (int i = 0; i < TABLE_COUNT; ++i)
+        if (TABLES[i].pi == pi && TABLES[i].log_n == log_n) {
+            *out = TABLES[i];
+            pthread_mutex_unlock(&TABLE_LOCK);
+            return 1;
+        }
+    int ok;
+    if (TABLE_COUNT < MAX_TABLES && TABLE_BYTES + bytes <= TABLE_BUDGET) {
+        ok = build_tables(&TABLES[TABLE_COUNT], prime, log_n);
+        if (ok) {
+            TABLES[TABLE_COUNT].cached = 1;
+            TABLE_BYTES += bytes;
+            *out = TABLES[TABLE_COUNT++];
+        }
+        pthread_mutex_unlock(&TABLE_LOCK);
+        return ok;
+    }
+    pthread_mutex_unlock(&TABLE_LOCK);
+    ok = build_tables(out, prime, log_n);
+    out->cached = 0;
+    return ok;
+}
+
+static void level_tables_release(LevelTables* t) {
+    if (t->cached) return;
+    free(t->fwd);
+    free(t->inv);
+}
+
+/* One radix-4 DIF step, half-sizes 2q then q, on x[j], x[j+q], x[j+2q], x[j+3q]
+ * for j < count: w1 = roots of half-size 2q at j, w1h at j + q, w2 = roots of
+ * half-size q at j. */
+static void dif4_q(double* restrict x0, double* restrict x1, double* restrict x2, double* restrict x3, u64 count,
+                   const double* restrict w1, const double* restrict w1h, const double* restrict w2, double p,
+                   double pinv) {
+    for (u64 j = 0; j < count; ++j) {
+        const double a0 = x0[j], a1 = x1[j], a2 = x2[j], a3 = x3[j];
+        const double b0 = reduce_c(a0 + a2, p, pinv), b2 = mul_c(a0 - a2, w1[j], p, pinv);
+        const double b1 = reduce_c(a1 + a3, p, pinv), b3 = mul_c(a1 - a3, w1h[j], p, pinv);
+        x0[j] = reduce_c(b0 + b1, p, pinv);
+        x1[j] = mul_c(b0 - b1, w2[j], p, pinv);
+        x2[j] = reduce_c(b2 + b3, p, pinv);
+        x3[j] = mul_c(b2 - b3, w2[j], p, pinv);
+    }
+}
+
+/* One radix-4 DIT step, half-sizes q then 2q (the inverse of dif4's shape). */
+static void dit4_q(double* restrict x0, double* restrict x1, double* restrict x2, double* restrict x3, u64 count,
+                   const double* restrict w2, const double* restrict w1, const double* restrict w1h, double p,
+                   double pinv) {
+    for (u64 j = 0; j < count; ++j) {
+        const double a0 = x0[j], a1 = x1[j], a2 = x2[j], a3 = x3[j];
+        const double t1 = mul_c(a1, w2[j], p, pinv), t3 = mul_c(a3, w2[j], p, pinv);
+        const double b0 = reduce_c(a0 + t1, p, pinv), b1 = reduce_c(a0 - t1, p, pinv);
+        const double b2 = reduce_c(a2 + t3, p, pinv), b3 = reduce_c(a2 - t3, p, pinv);
+        const double u = mul_c(b2, w1[j], p, pinv), v = mul_c(b3, w1h[j], p, pinv);
+        x0[j] = reduce_c(b0 + u, p, pinv);
+        x2[j] = reduce_c(b0 - u, p, pinv);
+        x1[j] = reduce_c(b1 + v, p, pinv);
+        x3[j] = reduce_c(b1 - v, p, pinv);
+    }
+}
+
+/* The quarters of x as separate restrict-qualified arrays (count <= q). */
+static void dif4(double* x, u64 q, u64 count, const double* w1, const double* w1h, const double* w2, double p,
+                 double pinv) {
+    dif4_q(x, x + q, x + 2 * q, x + 3 * q, count, w1, w1h, w2, p, pinv);
+}
+static void dit4(double* x, u64 q, u64 count, const double* w2, const double* w1, const double* w1h, double p,
+                 double pinv) {
+    dit4_q(x, x + q, x + 2 * q, x + 3 * q, count, w2, w1, w1h, p, pinv);
+}
+
+/* The last two DIF levels (half-sizes 2 and 1) of every group of four, vectorised
+ * across groups (stride-4 loads and stores). */
+static void dif4_leaf(double* restrict a, u64 m, const double* L, double p, double pinv) {
+    const double c1 = L[1], c2 = L[2], c3 = L[3];
+    for (u64 i = 0; i < m; i += 4) {
+        const double a0 = a[i], a1 = a[i + 1], a2 = a[i + 2], a3 = a[i + 3];
+        const double b0 = reduce_c(a0 + a2, p, pinv), b2 = mul_c(a0 - a2, c2, p, pinv);
+        const double b1 = reduce_c(a1 + a3, p, pinv), b3 = mul_c(a1 - a3, c3, p, pinv);
+        a[i] = reduce_c(b0 + b1, p, pinv);
+        a[i + 1] = mul_c(b0 - b1, c1, p, pinv);
+        a[i + 2] = reduce_c(b2 + b3, p, pinv);
+        a[i + 3] = mul_c(b2 - b3, c1, p, pinv);
+    }
+}
+static void dit4_leaf(double* restrict a, u64 m, const double* IL, double p, double pinv) {
+    const double c1 = IL[1], c2 = IL[2], c3 = IL[3];
+    for (u64 i = 0; i < m; i += 4) {
+        const double a0 = a[i], a1 = a[i + 1], a2 = a[i + 2], a3 = a[i + 3];
+        const double t1 = mul_c(a1, c1, p, pinv), t3 = mul_c(a3, c1, p, pinv);
+        const double b0 = reduce_c(a0 + t1, p, pinv), b1 = reduce_c(a0 - t1, p, pinv);
+        const double b2 = reduce_c(a2 + t3, p, pinv), b3 = reduce_c(a2 - t3, p, pinv);
+        const double u = mul_c(b2, c2, p, pinv), v = mul_c(b3, c3, p, pinv);
+        a[i] = reduce_c(b0 + u, p, pinv);
+        a[i + 2] = reduce_c(b0 - u, p, pinv);
+        a[i + 1] = reduce_c(b1 + v, p, pinv);
+        a[i + 3] = reduce_c(b1 - v, p, pinv);
+    }
+}
+
+static int log2_u64(u64 m) { return 63 - clz_u64(m); }
+
+/* One radix-2 level of half-size h over a[0, m). */
+static void dif2(double* a, u64 m, u64 h, const double* L, double p, double pinv) {
+    for (u64 blk = 0; blk < m; blk += 2 * h) {
+        double* restrict x = a + blk;
+        double* restrict y = x + h;
+        const double* w = L + h;
+        for (u64 j = 0; j < h; ++j) {
+            const double u = x[j], v = y[j];
+            x[j] = reduce_c(u + v, p, pinv);
+            y[j] = mul_c(u - v, w[j], p, pinv);
+        }
+    }
+}
+static void dit2(double* a, u64 m, u64 h, const double* IL, double p, double pinv) {
+    for (u64 blk = 0; blk < m; blk += 2 * h) {
+        double* restrict x = a + blk;
+        double* restrict y = x + h;
+        const double* w = IL + h;
+        for (u64 j = 0; j < h; ++j) {
+            const double t = mul_c(y[j], w[j], p, pinv);
+            const double u = x[j];
+            x[j] = reduce_c(u + t, p, pinv);
+            y[j] = reduce_c(u - t, p, pinv);
+        }
+    }
+}
+
+/* All DIF levels (half-sizes m/2 down to 1) of a[0, m) in cache: one radix-2
+ * level first when log2 m is odd, then radix-4 steps, the last across groups. */
+static void dif_block(double* a, u64 m, const double* L, double p, double pinv) {
+    if (m < 2) return;
+    u64 s = m;
+    if (log2_u64(m) & 1) {
+        dif2(a, m, m / 2, L, p, pinv);
+        s = m / 2;
+    }
+    for (; s >= 16; s /= 4)
+        for (u64 blk = 0; blk < m; blk += s) {
+            const u64 q = s / 4;
+            dif4(a + blk, q, q, L + 2 * q, L + 3 * q, L + q, p, pinv);
+        }
+    if (s == 4) dif4_leaf(a, m, L, p, pinv);
+}
+
+/* All DIT levels (half-sizes 1 up to m/2) of a[0, m) in cache (unscaled). */
+static void dit_block(double* a, u64 m, const double* IL, double p, double pinv) {
+    if (m < 2) return;
+    const int lg = log2_u64(m);
+    if (lg >= 2) {
+        dit4_leaf(a, m, IL, p, pinv);
+        for (u64 s = 16; s <= (1ull << (lg & ~1)); s *= 4)
+            for (u64 blk = 0; blk < m; blk += s) {
+                const u64 q = s / 4;
+                dit4(a + blk, q, q, IL + q, IL + 2 * q, IL + 3 * q, p, pinv);
+            }
+    }
+    if (lg & 1) dit2(a, m, m / 2, IL, p, pinv);
+}
+
+/* Cyclic DIF of a[0, m), natural order in, bit-reversed order out (centred). */
+static void dif_rec(double* a, u64 m, const double* L, double p, double pinv) {
+    if (m <= (1ull << BLOCK_LOG)) {
+        dif_block(a, m, L, p, pinv);
+        return;
+    }
+    const u64 q = m / 4;
+    dif4(a, q, q, L + 2 * q, L + 3 * q, L + q, p, pinv);
+    for (int k = 0; k < 4; ++k) dif_rec(a + k * q, q, L, p, pinv);
+}
+
+/* Cyclic DIT of a[0, m), bit-reversed order in, natural order out (unscaled). */
+static void dit_rec(double* a, u64 m, const double* IL, double p, double pinv) {
+    if (m <= (1ull << BLOCK_LOG)) {
+        dit_block(a, m, IL, p, pinv);
+        return;
+    }
+    const u64 q = m / 4;
+    for (int k = 0; k < 4; ++k) dit_rec(a + k * q, q, IL, p, pinv);
+    dit4(a, q, q, IL + q, IL + 2 * q, IL + 3 * q, p, pinv);
+}
+
+/* One prime's cyclic product in the spectrum (src/multiply/schedule.rs:18 and the
+ * fused leaf schedules of src/arch/schedule/ restated): below the cache block each
+ * sub-transform of a and of b is finished, multiplied pointwise with the folded
+ * factor and inverted while it is in cache. */
+typedef struct {
+    const double *L, *IL;
+    double p, pinv, factor;
+    int square;
+} Ring;
+
+static void pointwise(double* restrict x, const double* y, u64 m, double factor, double p, double pinv) {
+    for (u64 i = 0; i < m; ++i) {
+        const double u = reduce_c(x[i], p, pinv), v = reduce_c(y[i], p, pinv);
+        x[i] = mul_c(mul_c(u, v, p, pinv), factor, p, pinv);
+    }
+}
+
+static void fused_rec(double* a, double* b, u64 m, const Ring* r) {
+    if (m <= (1ull << BLOCK_LOG)) {
+        dif_block(a, m, r->L, r->p, r->pinv);
+        if (!r->square) dif_block(b, m, r->L, r->p, r->pinv);
+        pointwise(a, r->square ? a : b, m, r->factor, r->p, r->pinv);
+        dit_block(a, m, r->IL, r->p, r->pinv);
+        return;
+    }
+    const u64 q = m / 4;
+    dif4(a, q, q, r->L + 2 * q, r->L + 3 * q, r->L + q, r->p, r->pinv);
+    if (!r->square) dif4(b, q, q, r->L + 2 * q, r->L + 3 * q, r->L + q, r->p, r->pinv);
+    for (int k = 0; k < 4; ++k) fused_rec(a + k * q, b + k * q, q, r);
+    dit4(a, q, q, r->IL + q, r->IL + 2 * q, r->IL + 3 * q, r->p, r->pinv);
+}
+
+/* The fast transforms on canonical input, canonical output. */
+static int ntt_forward_fast(double* a, const Field* f) {
+    int log_n = 0;
+    while ((1ull << log_n) < f->n) ++log_n;
+    LevelTables t;
+    if (!level_tables(f->prime, log_n, &t)) return 0;
+    dif_rec(a, f->n, t.fwd, f->p, f->pinv);
+    for (u64 i = 0; i < f->n; ++i) a[i] = canon_c(a[i], f->p);
+    level_tables_release(&t);
+    return 1;
+}
+static int ntt_inverse_fast(double* a, const Field* f) {
+    int log_n = 0;
+    while ((1ull << log_n) < f->n) ++log_n;
+    LevelTables t;
+    if (!level_tables(f->prime, log_n, &t)) return 0;
+    dit_rec(a, f->n, t.inv, f->p, f->pinv);
+    for (u64 i = 0; i < f->n; ++i) a[i] = canon_c(a[i], f->p);
+    level_tables_release(&t);
+    return 1;
+}
+
 /* Bits [pos, pos+len) of a limb vector (len <= 64); zero past the end. */
 static inline u64 get_bits(const u64* limbs, u64 count, u64 pos, int len) {
     const u64 li = pos >> 6;
@@ -504,32 +847,6 @@ static inline u64 get_bits(const u64* limbs, u64 count, u64 pos, int len) {
     u64 v = limbs[li] >> off;
     if (off && li + 1 < count) v |= limbs[li + 1] << (64 - off);
     return len == 64 ? v : v & ((1ull << len) - 1);
-}
-
-/* Packing::pack, src/limb/packing.rs:113-301: coefficient k is bits
- * [k*w, k*w+w), reduced as sum_k part_k * (2^(49k) mod p). Signed geometries
- * read each limb as two's complement. */
-static void pack_row(double* row, const u64* limbs, u64 count, u64 digits, const Geometry* g, const Field* f,
-                     int prime, int is_signed) {
-    const int w = g->chunk_bits;
-    double pw[MAX_PARTS];
-    for (int k = 0; k < MAX_PARTS; ++k) pw[k] = (double)powmod_int(2, (u64)PART_BITS * k, CAT_P[prime]);
-    const double two64 = (double)powmod_int(2, 64, CAT_P[prime]);
-    for (u64 i = 0; i < f->n; ++i) {
-        if (i >= digits) {
-            row[i] = 0.0;
-            continue;
-        }
-        double r = 0.0;
-        const u64 base = i * (u64)w;
-        for (int part = 0; part * PART_BITS < w; ++part) {
-            const int len = (w - part * PART_BITS) < PART_BITS ? (w - part * PART_BITS) : PART_BITS;
-            const u64 bits = get_bits(limbs, count, base + (u64)part * PART_BITS, len);
-            r = addmod(r, fmulmod((double)bits, pw[part], f->p, f->pinv), f->p);
-        }
-        if (is_signed && (int64_t)limbs[i] < 0) r = submod(r, two64, f->p);
-        row[i] = r;
-    }
 }
 
 /* ------------------------------------------------------------------------------
@@ -568,7 +885,14 @@ static void run_tasks(void (*fn)(void*, int), void* ctx, int tasks, int threads)
 }
 
 /* ------------------------------------------------------------------------------
- * One multiplication under a geometry */
+ * One multiplication under a geometry, in phases that each split into independent
+ * tasks for the pool (the rayon joins of src/transform/forward.rs and
+ * src/multiply/schedule.rs): digit parts of each operand, per-prime rows, the top
+ * TOP_PASSES radix-4 steps of every forward transform, the fused leaf products of
+ * the 4^TOP_PASSES sub-transforms, the top inverse steps, reconstruction. */
+#define TOP_PASSES 2
+#define TASK_SPAN 16384 /* elements per task of a streaming phase */
+
 typedef struct {
     const Geometry* g;
     const u64 *a, *b;
@@ -576,11 +900,19 @@ typedef struct {
     int square;
     int is_signed;
     u64 n;
+    int ops; /* 1 for a square */
     Field* fields;
+    LevelTables tab[MAX_PRIMES];
+    double factor[MAX_PRIMES];
+    double* parts[2]; /* [part][digit] of each operand */
+    int nparts;
     double** spec_a;
     double** spec_b;
+    int top;  /* radix-4 steps above the fused leaves */
+    int pass; /* the top step in progress: sub-transforms of n >> 2*pass */
     /* reconstruction */
     const Cofactors* cof;
+    u64 off[MAX_PRIMES]; /* residues of 2^sign_bit (P/p_i)^-1 */
     u64* out;
     u64 out_len;
     u64 range;  /* coefficients per reconstruction task */
@@ -590,29 +922,100 @@ typedef struct {
     int tasks;
 } Job;
 
-static void task_forward(void* ctx, int t) {
+static u64 spans(u64 len) { return len > TASK_SPAN ? div_ceil(len, TASK_SPAN) : 1; }
+
+/* Digit parts (Packing::pack's 49-bit parts, src/limb/packing.rs:113-301). */
+static void task_parts(void* ctx, int t) {
     Job* j = (Job*)ctx;
-    const int prime = t >> 1, op = t & 1;
-    if (op && j->square) return;
-    const Field* f = &j->fields[prime];
-    if (op == 0)
-        pack_row(j->spec_a[prime], j->a, j->la, j->g->digits_a, j->g, f, prime, j->is_signed);
-    else
-        pack_row(j->spec_b[prime], j->b, j->lb, j->g->digits_b, j->g, f, prime, j->is_signed);
-    ntt_forward(op ? j->spec_b[prime] : j->spec_a[prime], f);
+    const u64 per = spans(j->n);
+    const int op = (int)(t / per);
+    const u64 digits = op ? j->g->digits_b : j->g->digits_a;
+    const u64* limbs = op ? j->b : j->a;
+    const u64 count = op ? j->lb : j->la;
+    const int w = j->g->chunk_bits;
+    const u64 i0 = (t % per) * TASK_SPAN;
+    const u64 i1 = i0 + TASK_SPAN < digits ? i0 + TASK_SPAN : digits;
+    for (int part = 0; part < j->nparts; ++part) {
+        const int len = (w - part * PART_BITS) < PART_BITS ? (w - part * PART_BITS) : PART_BITS;
+        double* dst = j->parts[op] + (u64)part * j->n;
+        for (u64 i = i0; i < i1; ++i)
+            dst[i] = (double)get_bits(limbs, count, i * (u64)w + (u64)part * PART_BITS, len);
+    }
 }
 
-/* Pointwise product and inverse; the factor N^-1 (P/p_i)^-1 folds into the
- * pointwise product as src/multiply/schedule.rs:236-252 folds it. */
-static void task_inverse(void* ctx, int prime) {
+/* A prime's row: sum_k part_k * (2^(49k) mod p), centred; signed geometries read
+ * each limb as two's complement. */
+static void task_rows(void* ctx, int t) {
     Job* j = (Job*)ctx;
+    const u64 per = spans(j->n);
+    const int row = (int)(t / per);
+    const int prime = row / j->ops, op = row % j->ops;
     const Field* f = &j->fields[prime];
-    double* x = j->spec_a[prime];
-    const double* y = j->square ? x : j->spec_b[prime];
-    const u64 ninv = powmod_int(j->n % f->pi, f->pi - 2, f->pi);
-    const double factor = (double)mulmod_int(ninv, j->cof->inverses[prime], f->pi);
-    for (u64 i = 0; i < j->n; ++i) x[i] = fmulmod(fmulmod(x[i], y[i], f->p, f->pinv), factor, f->p, f->pinv);
-    ntt_inverse(x, f);
+    const double p = f->p, pinv = f->pinv;
+    const u64 digits = op ? j->g->digits_b : j->g->digits_a;
+    const u64* limbs = op ? j->b : j->a;
+    double* dst = op ? j->spec_b[prime] : j->spec_a[prime];
+    double pw[MAX_PARTS];
+    for (int k = 0; k < MAX_PARTS; ++k) {
+        const u64 c = powmod_int(2, (u64)PART_BITS * k, f->pi);
+        pw[k] = c > f->pi / 2 ? (double)c - p : (double)c;
+    }
+    const u64 c64 = powmod_int(2, 64, f->pi);
+    const double two64 = c64 > f->pi / 2 ? (double)c64 - p : (double)c64;
+    const u64 i0 = (t % per) * TASK_SPAN;
+    const u64 i1 = i0 + TASK_SPAN < j->n ? i0 + TASK_SPAN : j->n;
+    const u64 d1 = digits < i1 ? (digits > i0 ? digits : i0) : i1;
+    /* part 0 is below 2^49 < p/2, already centred; each further term lies in
+     * (-0.75p, 0.75p), so the sum stays below 2.75p before the reduction */
+    const double* src = j->parts[op];
+    for (u64 i = i0; i < d1; ++i) dst[i] = src[i];
+    for (int k = 1; k < j->nparts; ++k) {
+        const double* restrict part = src + (u64)k * j->n;
+        double* restrict out = dst;
+        const double c = pw[k];
+        for (u64 i = i0; i < d1; ++i) out[i] += mul_c(part[i], c, p, pinv);
+    }
+    for (u64 i = i0; i < d1; ++i) dst[i] = reduce_c(dst[i], p, pinv);
+    if (j->is_signed)
+        for (u64 i = i0; i < d1; ++i)
+            if ((int64_t)limbs[i] < 0) dst[i] = reduce_c(dst[i] - two64, p, pinv);
+    for (u64 i = d1; i < i1; ++i) dst[i] = 0.0;
+}
+
+/* Task t of the top step `pass`: (prime, operand, sub-transform, span of j). */
+static void task_forward_top(void* ctx, int t) {
+    Job* j = (Job*)ctx;
+    const u64 m = j->n >> (2 * j->pass), q = m / 4, per = spans(q), blocks = 1ull << (2 * j->pass);
+    const u64 span = (u64)t % per, blk = ((u64)t / per) % blocks;
+    const int row = (int)((u64)t / per / blocks);
+    const int prime = row / j->ops, op = row % j->ops;
+    const Field* f = &j->fields[prime];
+    const double* L = j->tab[prime].fwd;
+    const u64 j0 = span * TASK_SPAN, cnt = j0 + TASK_SPAN < q ? TASK_SPAN : q - j0;
+    double* x = (op ? j->spec_b[prime] : j->spec_a[prime]) + blk * m + j0;
+    dif4(x, q, cnt, L + 2 * q + j0, L + 3 * q + j0, L + q + j0, f->p, f->pinv);
+}
+
+static void task_leaves(void* ctx, int t) {
+    Job* j = (Job*)ctx;
+    const u64 blocks = 1ull << (2 * j->top), m = j->n >> (2 * j->top);
+    const int prime = (int)((u64)t / blocks);
+    const u64 blk = (u64)t % blocks;
+    const Field* f = &j->fields[prime];
+    const Ring r = {j->tab[prime].fwd, j->tab[prime].inv, f->p, f->pinv, j->factor[prime], j->square};
+    fused_rec(j->spec_a[prime] + blk * m, j->square ? NULL : j->spec_b[prime] + blk * m, m, &r);
+}
+
+static void task_inverse_top(void* ctx, int t) {
+    Job* j = (Job*)ctx;
+    const u64 m = j->n >> (2 * j->pass), q = m / 4, per = spans(q), blocks = 1ull << (2 * j->pass);
+    const u64 span = (u64)t % per, blk = ((u64)t / per) % blocks;
+    const int prime = (int)((u64)t / per / blocks);
+    const Field* f = &j->fields[prime];
+    const double* IL = j->tab[prime].inv;
+    const u64 j0 = span * TASK_SPAN, cnt = j0 + TASK_SPAN < q ? TASK_SPAN : q - j0;
+    double* x = j->spec_a[prime] + blk * m + j0;
+    dit4(x, q, cnt, IL + q + j0, IL + 2 * q + j0, IL + 3 * q + j0, f->p, f->pinv);
 }
 
 /* Adds `words` words of v shifted left by `shift` bits at limb `at` of dst[0..len). */
@@ -640,13 +1043,9 @@ static void reconstruct_coefficient(const Job* j, u64 k, u64* value) {
     const int count = j->g->count;
     u64 r[MAX_PRIMES];
     for (int i = 0; i < count; ++i) {
-        r[i] = (u64)j->spec_a[i][k];
-        if (j->g->sign_bit >= 0) {
-            /* residue of 2^s times the inverse, src/limb/reconstruction.rs:94-113 */
-            const u64 p = CAT_P[i];
-            const u64 off = mulmod_int(powmod_int(2, (u64)j->g->sign_bit, p), j->cof->inverses[i], p);
-            r[i] = (r[i] + off) % p;
-        }
+        r[i] = (u64)canon_c(j->spec_a[i][k], j->fields[i].p);
+        /* residue of 2^s times the inverse, src/limb/reconstruction.rs:94-113 */
+        if (j->g->sign_bit >= 0) r[i] = (r[i] + j->off[i]) % CAT_P[i];
     }
     cof_bounded(j->cof, count, r, value);
 }
@@ -708,28 +1107,54 @@ static int multiply_under(const Geometry* g, u64* out, u64 out_len, const u64* a
     j.la = la;
     j.lb = lb;
     j.square = square;
+    j.ops = square ? 1 : 2;
     j.is_signed = is_signed;
     u64 n = next_pow2(g->conv_len);
     if (n < MIN_TRANSFORM_LEN) n = MIN_TRANSFORM_LEN;
     j.n = n;
     j.cof = cof_of(g->count);
+    j.nparts = (g->chunk_bits + PART_BITS - 1) / PART_BITS;
     const int count = g->count;
+    const int log_n = log2_u64(n);
     Field fields[MAX_PRIMES];
     double* sa[MAX_PRIMES] = {0};
     double* sb[MAX_PRIMES] = {0};
-    int ok = 1;
+    int ok = 1, have[MAX_PRIMES] = {0};
+    for (int op = 0; op < j.ops; ++op) {
+        j.parts[op] = (double*)malloc((size_t)j.nparts * n * sizeof(double));
+        ok &= j.parts[op] != NULL;
+    }
     for (int i = 0; i < count; ++i) {
-        ok &= field_init(&fields[i], i, n);
+        ok &= field_init(&fields[i], i, n, 0);
+        have[i] = level_tables(i, log_n, &j.tab[i]);
+        ok &= have[i];
         sa[i] = (double*)malloc(n * sizeof(double));
         sb[i] = square ? NULL : (double*)malloc(n * sizeof(double));
         ok &= sa[i] != NULL && (square || sb[i] != NULL);
+        /* N^-1 (P/p_i)^-1 folds into the pointwise product (src/multiply/schedule.rs:236-252) */
+        const u64 pi = CAT_P[i];
+        const u64 ninv = powmod_int(n % pi, pi - 2, pi);
+        const u64 fac = mulmod_int(ninv, j.cof->inverses[i], pi);
+        j.factor[i] = fac > pi / 2 ? (double)fac - (double)pi : (double)fac;
+        if (g->sign_bit >= 0)
+            j.off[i] = mulmod_int(powmod_int(2, (u64)g->sign_bit, pi), j.cof->inverses[i], pi);
     }
     if (ok) {
         j.fields = fields;
         j.spec_a = sa;
         j.spec_b = sb;
-        run_tasks(task_forward, &j, 2 * count, threads);
-        run_tasks(task_inverse, &j, count, threads);
+        for (u64 m = n; j.top < TOP_PASSES && m > (1ull << BLOCK_LOG); m /= 4) ++j.top;
+        run_tasks(task_parts, &j, (int)(j.ops * spans(n)), threads);
+        run_tasks(task_rows, &j, (int)(count * j.ops * spans(n)), threads);
+        for (j.pass = 0; j.pass < j.top; ++j.pass) {
+            const u64 q = (n >> (2 * j.pass)) / 4;
+            run_tasks(task_forward_top, &j, (int)(count * j.ops * (1ull << (2 * j.pass)) * spans(q)), threads);
+        }
+        run_tasks(task_leaves, &j, (int)(count * (1ull << (2 * j.top))), threads);
+        for (j.pass = j.top - 1; j.pass >= 0; --j.pass) {
+            const u64 q = (n >> (2 * j.pass)) / 4;
+            run_tasks(task_inverse_top, &j, (int)(count * (1ull << (2 * j.pass)) * spans(q)), threads);
+        }
         j.out = out;
         j.out_len = out_len;
         const int tasks = threads > 1 ? 4 * threads : 1;
@@ -753,7 +1178,9 @@ static int multiply_under(const Geometry* g, u64* out, u64 out_len, const u64* a
         free(j.part_start);
         free(j.part_len);
     }
+    for (int op = 0; op < 2; ++op) free(j.parts[op]);
     for (int i = 0; i < count; ++i) {
+        if (have[i]) level_tables_release(&j.tab[i]);
         field_free(&fields[i]);
         free(sa[i]);
         free(sb[i]);
@@ -860,4 +1287,36 @@ void oracle_operand(uint64_t* dst, uint64_t len, uint64_t seed) {
         z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
         dst[i] = z ^ (z >> 31);
     }
+}
+
+/* The cache-blocked transforms against the radix-2 ones on seeded canonical input:
+ * 1 when forward and inverse agree bit for bit (test infrastructure). */
+int oracle_transform_check(int prime, int log_n, uint64_t seed) {
+    if (prime < 0 || prime >= MAX_PRIMES || log_n < 1 || log_n > 24) return -1;
+    const u64 n = 1ull << log_n;
+    Field f;
+    if (!field_init(&f, prime, n, 1)) return -1;
+    double* x = (double*)malloc(n * sizeof(double));
+    double* y = (double*)malloc(n * sizeof(double));
+    int same = x && y;
+    u64 st = seed;
+    for (u64 i = 0; same && i < n; ++i) {
+        st += 0x9E3779B97F4A7C15ull;
+        u64 z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        x[i] = y[i] = (double)((z ^ (z >> 31)) % f.pi);
+    }
+    if (same) {
+        ntt_forward(x, &f);
+        same = ntt_forward_fast(y, &f);
+        for (u64 i = 0; same && i < n; ++i) same = x[i] == y[i];
+        ntt_inverse(x, &f);
+        same = same && ntt_inverse_fast(y, &f);
+        for (u64 i = 0; same && i < n; ++i) same = x[i] == y[i];
+    }
+    free(x);
+    free(y);
+    field_free(&f);
+    return same;
 }

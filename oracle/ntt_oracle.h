@@ -16,4 +16,5 @@ int oracle_row_shape(uint64_t conv_len, uint64_t longest, uint64_t* out3);
 int oracle_capacity(int count);
 void oracle_schoolbook(uint64_t* dst, const uint64_t* a, uint64_t la, const uint64_t* b, uint64_t lb);
 void oracle_operand(uint64_t* dst, uint64_t len, uint64_t seed);
+int oracle_transform_check(int prime, int log_n, uint64_t seed);
 #endif

@@ -117,3 +117,12 @@ def test_every_prefix_at_capacity():
             mb = (1 << 64) - 1 if cap > 64 else 1
             plan = oracle.conv_plan(1, 1, ma, mb, False)
             assert plan["primes"] <= count
+
+
+def test_cache_blocked_transforms_equal_radix_2():
+    # the timed CPU path's transforms (cache-blocked, radix-4 above the block, lazy
+    # centred residues) against the plain radix-2 ones, bit for bit, across the
+    # block boundary and for every catalog prime
+    for prime in range(8):
+        for log_n in (1, 2, 5, 11, 12, 13, 14, 15, 17):
+            assert oracle.transform_check(prime, log_n, 7 + prime + log_n), (prime, log_n)
