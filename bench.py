@@ -205,6 +205,30 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+KERNEL_NAMES = ["pack+column DIF (k_fwd_cols)", "row DIF+pointwise+DIT (k_rows)", "column DIT (k_inv_cols)",
+                "CRT+window sums+look-back carry (k_crt_mul)"]
+
+
+def kernel_breakdown(run, reps: int):
+    """Device time of each of a four-step product's kernels, from CUDA events the
+    library records between its launches (ntt_timing_start/stop), averaged over
+    `reps` products; None if the call did not take the four-kernel path."""
+    import ctypes
+
+    import nttanafis_gb300 as ntt
+
+    lib = ntt.library()
+    stride = len(KERNEL_NAMES) + 1
+    ms = (ctypes.c_float * (reps * stride))()
+    lib.ntt_timing_start(reps * stride)
+    for _ in range(reps):
+        run()
+    got = lib.ntt_timing_stop(ms, reps * stride)
+    if got != reps * stride - 1:
+        return None
+    return {n: round(sum(ms[r * stride + k] for r in range(reps)) / reps, 5) for k, n in enumerate(KERNEL_NAMES)}
+
+
 def configs_section(dev, stream, peak_gbs: float) -> list:
     """Device time per product of every plain configuration (inputs resident), with
     its algorithmic bytes and roofline fraction. Squares pass the same tensor twice."""
@@ -228,6 +252,7 @@ def configs_section(dev, stream, peak_gbs: float) -> list:
         ("mul 4194304x4194304", 1 << 22, 1 << 22, operand, 20),
         ("mul 16777216x16777216", 1 << 24, 1 << 24, operand, 6), ("sqr 16777216", 1 << 24, 0, operand, 6),
     ]
+    broken_down = {"mul 1048576x1048576", "sqr 1048576", "mul 16777216x16777216", "sqr 16777216"}
     ws = ntt.GpuMulWorkspace()
     out = []
     for name, la, lb, gen, reps in cases:
@@ -246,8 +271,11 @@ def configs_section(dev, stream, peak_gbs: float) -> list:
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / reps
         model = oracle.model_bytes("sqr" if lb == 0 else "mul", la, lb or la)
-        out.append({"config": name, "ms_per_product": round(ms, 5), "products_per_s": round(1000.0 / ms, 1),
-                    "algorithmic_bytes": model, "roofline_frac": round(model / (ms / 1000.0) / 1e9 / peak_gbs, 4)})
+        row = {"config": name, "ms_per_product": round(ms, 5), "products_per_s": round(1000.0 / ms, 1),
+               "algorithmic_bytes": model, "roofline_frac": round(model / (ms / 1000.0) / 1e9 / peak_gbs, 4)}
+        if name in broken_down:
+            row["kernels_ms"] = kernel_breakdown(lambda: ws.mul_device(d, a, b, stream), min(reps, 10))
+        out.append(row)
         del a, b, d
     ws.close()
     # Convolutions of 16-bit coefficients (the reference's published conv sizes,
@@ -621,8 +649,7 @@ def run_gpu(args) -> None:
     e2e_value = world * e2e_steps / max_over_ranks(e2e_s, world, dev)
 
     # Per-kernel device times: events recorded between the library's launches.
-    kernel_names = ["pack+column DIF (k_fwd_cols)", "row DIF+pointwise+DIT (k_rows)",
-                    "column DIT (k_inv_cols)", "CRT+window sums+look-back carry (k_crt_mul)"]
+    kernel_names = KERNEL_NAMES
     import ctypes
 
     reps = 10

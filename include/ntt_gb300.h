@@ -220,6 +220,10 @@ int ntt_batch_set_lanes(ntt_batch* batch, int lanes);
 /* out[0] runs served from a captured graph, out[1] compositions tuned, out[2]
  * lanes of the last run enqueued directly or captured, out[3] compositions held. */
 void ntt_batch_stats(const ntt_batch* batch, uint64_t* out);
+/* Products of the batch's runs that ran as block splits (an operand many times
+ * longer than the other: the shorter operand's spectrum once per run, the longer
+ * operand's blocks multiplied by it, as MulPlan's split products do). */
+uint64_t ntt_batch_split_members(const ntt_batch* batch);
 /* NTT_STATUS_* bits of the batch's runs since the last query, cleared by reading;
  * call it after the runs' stream has completed. A convolution member with a
  * coefficient above its bound is left unwritten (the other members complete). */

@@ -104,6 +104,7 @@ _SIGNATURES = [
     ("ntt_batch_set_lanes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     ("ntt_batch_stats", None, [ctypes.c_void_p, ctypes.c_void_p]),
     ("ntt_batch_status", ctypes.c_uint32, [ctypes.c_void_p]),
+    ("ntt_batch_split_members", ctypes.c_uint64, [ctypes.c_void_p]),
     ("ntt_mul_noalloc_device", ctypes.c_uint8,
      [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
       ctypes.c_void_p]),
@@ -555,6 +556,11 @@ class GpuBatch:
         """STATUS_* bits of this batch's runs since the last query (0: every member
         succeeded); read after the runs' stream has completed. Reading clears them."""
         return int(self._lib.ntt_batch_status(self._b))
+
+    @property
+    def split_members(self) -> int:
+        """Products of this batch object's runs that ran as block splits."""
+        return int(self._lib.ntt_batch_split_members(self._b))
 
     @property
     def graph_replays(self) -> int:

@@ -75,6 +75,7 @@ struct ntt_batch {
     uint64_t clock = 0;
     uint64_t replays = 0;
     uint64_t tuned = 0;
+    uint64_t split_members = 0;  // products run as block splits
     std::map<std::vector<uint64_t>, Composition> comps;
 };
 
@@ -145,6 +146,8 @@ uint32_t ntt_batch_status(ntt_batch* b) {
     if (bits) *reinterpret_cast<volatile u32*>(b->status_host) = 0;
     return bits;
 }
+
+uint64_t ntt_batch_split_members(const ntt_batch* b) { return b ? b->split_members : 0; }
 
 void ntt_batch_stats(const ntt_batch* b, uint64_t* out) {
     if (!out) return;
@@ -355,6 +358,7 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
     std::vector<Member> members;
     members.reserve(count);
     std::vector<size_t> empties;
+    std::vector<Member> splits;  // unbalanced products: block splits, enqueued one by one
     u64 arena_bytes = 0;
     for (size_t i = 0; i < count; ++i) {
         const ntt_request& r = reqs[i];
@@ -366,7 +370,7 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
                 empties.push_back(i);
                 continue;
             }
-            if (!plan_mul(r.a_len, r.b_len, m.g, false)) return 0;
+            if (!plan_mul(r.a_len, r.b_len, m.g, true)) return 0;
         } else if (r.kind == 1) {
             if (!plan_conv(r.a_len, r.b_len, r.max_a, r.max_b, (int)r.is_signed, m.g)) return 0;
         } else {
@@ -376,12 +380,12 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         m.square = r.a == r.b && r.a_len == r.b_len;
         m.offset = arena_bytes;
         arena_bytes += (m.g.scratch_bytes(m.square) + 255) & ~(u64)255;
-        members.push_back(m);
+        (m.g.split() ? splits : members).push_back(m);
     }
     for (size_t i : empties)
         if (!cuda_ok(cudaMemsetAsync(reqs[i].dst, 0, ((size_t)reqs[i].a_len + reqs[i].b_len) * 8, st), "zero product"))
             return 0;
-    if (members.empty()) return 1;
+    if (members.empty() && splits.empty()) return 1;
     // Group by class: kind, schoolbook, transform length, primes, sign, square.
     std::sort(members.begin(), members.end(), [](const Member& x, const Member& y) {
         return std::make_tuple(x.g.conv, x.g.schoolbook, x.g.log_t, x.g.np, x.g.sign, x.square, x.index) <
@@ -391,6 +395,17 @@ uint8_t ntt_batch_run_device(ntt_batch* b, const ntt_request* reqs, size_t count
         return 0;
     if (b->pending && !cuda_ok(cudaEventSynchronize(b->staged), "descriptor staging")) return 0;
     b->pending = false;
+    // A product that the planner splits (one operand many times longer than the
+    // other) runs as its own block split: the shorter operand's spectrum once, the
+    // longer operand's blocks as members of one class (exec.cu), in its arena slot.
+    for (const Member& m : splits) {
+        const ntt_request& r = reqs[m.index];
+        if (!execute(m.g, false, r.a, r.b, r.dst, (uint8_t*)b->arena.ptr + m.offset, st, nullptr, b->status_dev,
+                     false))
+            return 0;
+        ++b->split_members;
+    }
+    if (members.empty()) return 1;
     if (b->host_cap < members.size()) {
         if (b->host_desc) cudaFreeHost(b->host_desc);
         b->host_desc = nullptr;

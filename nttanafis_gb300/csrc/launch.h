@@ -35,6 +35,14 @@ __host__ __device__ constexpr int col_group_log(int log_r) {
     return log_r + kColLogG >= 12 ? kColLogG : 12 - log_r;
 }
 __host__ __device__ constexpr int col_log_rs(int log_r) { return 8 - col_group_log(log_r); }
+// Columns of 2^12 points (the wide lengths T = 2^24, 2^25) run as two radix-64
+// passes (k_fwd_cols4, k_inv_cols4 in transform.cu): 8 columns per CTA of 512
+// threads, 64 points per thread and pass.
+constexpr int kCol4LogR = 12, kCol4Threads = 512;
+// log2 of the f4_a entries per column: the first factor of the forward four-step
+// twiddle of row r is indexed by the top log_u bits of brev(r), the second (f4_b)
+// by the rest.
+__host__ __device__ constexpr int step_log_u(int log_r) { return log_r == kCol4LogR ? 6 : col_log_rs(log_r); }
 // Four-step twiddles, tabulated per prime and transform length T = R * C:
 //  - forward, applied by the column pass: w_T^(col * brev(row)). Row r0 + RS*k has
 //    the bit-reversed index brev(r0) * SW + brev(k), so the twiddle is
@@ -227,8 +235,8 @@ struct StepTableBuild {
 __host__ __device__ inline void step_table_sizes(int log_t, int log_r, u64 sizes[4]) {
     const int log_c = log_t - log_r;
     const u64 R = (u64)1 << log_r, C = (u64)1 << log_c;
-    sizes[0] = C << col_log_rs(log_r);             // f4_a: [col][brev(r0)]
-    sizes[1] = C * (R >> col_log_rs(log_r));       // f4_b: [col][sweep]
+    sizes[0] = C << step_log_u(log_r);             // f4_a: [col][u]
+    sizes[1] = C * (R >> step_log_u(log_r));       // f4_b: [col][j]
     sizes[2] = R << kRowTwLoBits;                  // i4_lo: [row][lo]
     sizes[3] = R * (C >> kRowTwLoBits);            // i4_hi: [row][hi]
 }

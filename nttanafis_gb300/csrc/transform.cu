@@ -290,6 +290,126 @@ __global__ void __launch_bounds__(kThreads, NTT_INV_COLS2_MINB) k_inv_cols2(cons
     }
 }
 
+// Column passes for R = 2^12 (the wide lengths T = 2^24 and 2^25) in two radix-64
+// passes, the k_fwd_cols2 design at twice the block: 8 columns per CTA, 512
+// threads, thread t owning column c = t mod 8 and either rows blk + 64k (pass 1)
+// or rows 64 blk + k (pass 2), k < 64. Row r = 64a + b sits at slot 65a + b of its
+// column, whose stride (4 mod 32) puts a warp's 8 columns x 4 blocks on 32
+// distinct banks in both orders. The forward four-step twiddle of row 64 blk + k is
+// w_T^(col * brev(row)) = f4_a[col][brev6(k)] * f4_b[col][brev6(blk)]. The level
+// roots of the consecutive-point pass (entries 1..63) sit in shared memory.
+constexpr int kCol4Vs = 65 * 64 + 4;
+static_assert(kCol4Vs % 32 == 4 && step_log_u(kCol4LogR) == 6, "radix-64 column layout");
+
+static size_t col4_smem(bool fwd) {
+    return (size_t)8 * kCol4Vs * sizeof(u32) + 64 * sizeof(uint2) + (fwd ? 8 * 65 * sizeof(uint2) : 0);
+}
+
+template <class A, bool SIGNED>
+__global__ void __launch_bounds__(kCol4Threads, 1) k_fwd_cols4(const __grid_constant__ TransformArgs g) {
+    extern __shared__ u32 sm[];
+    release_dependents();
+    constexpr int G = 8, VS = kCol4Vs, E = 64;
+    const int prime = blockIdx.y;
+    const int op = g.batch ? (g.a_only ? 0 : blockIdx.z & 1) : blockIdx.z + g.op_base;
+    const Member m = member_of(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, false);
+    if (op && m.square) return;
+    const PrimeParams& pp = g.ps.pr[prime];
+    const u64* __restrict__ src = op ? m.b : m.a;
+    const u64 len = op ? m.lb : m.la;
+    const int log_c = g.log_c;
+    const u32 col0 = (u32)(blockIdx.x * G);
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    const u32 col = col0 + c;
+    uint2* tw = reinterpret_cast<uint2*>(sm + G * VS);
+    uint2* fa = tw + 64;  // f4_a rows of the CTA's columns, 65 entries apart
+    if (threadIdx.x < 64) tw[threadIdx.x] = __ldg(pp.fwd + threadIdx.x);
+    fa[c * (E + 1) + blk] = __ldg(pp.f4_a + ((size_t)col << 6) + blk);
+    // Pass 1: levels 0-5 on rows blk + 64k, limbs reduced on the way in; rows R/2
+    // and above hold no limb when len <= T/2.
+    {
+        const bool half = len <= ((u64)1 << (g.log_t - 1));
+        const u64* p0 = src + ((u64)blk << log_c) + col;
+        const u64 n0 = ((u64)blk << log_c) + col, kstep = (u64)E << log_c;
+        u32 x[1][E];
+        if (half) {
+#pragma unroll
+            for (int k = 0; k < E / 2; ++k)
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            dif_levels<A, 6, E, 1, true>(x, pp.fwd + blk, pp.p);
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; ++k)
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            dif_levels<A, 6, E, 1>(x, pp.fwd + blk, pp.p);
+        }
+        u32* base = sm + c * VS + blk;
+#pragma unroll
+        for (int k = 0; k < E; ++k) base[65 * k] = x[0][k];
+    }
+    __syncthreads();
+    // Pass 2: levels 6-11 on rows 64 blk + k, four-step twiddle, store.
+    {
+        const u32* base = sm + c * VS + 65 * blk;
+        u32 x[1][E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) x[0][k] = base[k];
+        // the last level (twiddle 1) stays open for the four-step product
+        dif_levels<A, 6, 1, 1, false, true>(x, tw, pp.p);
+        const uint2 fb = __ldg(pp.f4_b + ((size_t)col << 6) + (__brev((u32)blk) >> 26));
+        const uint2* fac = fa + c * (E + 1);
+        u32* dst = m.spec + ((size_t)(op * g.np + prime) << g.log_t) + ((u64)(blk * E) << log_c) + col;
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+            const u32 y = A::mulc(A::mulc(x[0][k], fac[__brev((u32)k) >> 26], pp.p), fb, pp.p);
+            dst[(u64)k << log_c] = y;
+        }
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kCol4Threads, 1) k_inv_cols4(const __grid_constant__ TransformArgs g) {
+    extern __shared__ u32 sm[];
+    constexpr int G = 8, VS = kCol4Vs, E = 64;
+    const int prime = blockIdx.y;
+    const PrimeParams& pp = g.ps.pr[prime];
+    const Member m = member_of(g, blockIdx.z, false);
+    release_dependents();
+    const int log_c = g.log_c;
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    uint2* tw = reinterpret_cast<uint2*>(sm + G * VS);
+    if (threadIdx.x < 64) tw[threadIdx.x] = __ldg(pp.inv + threadIdx.x);
+    __syncthreads();
+    wait_prior_grid();  // the row pass's output
+    // the CRT look-back flags of this product, cleared once every kernel before
+    // this one has completed
+    if (blockIdx.x == 0 && prime == 0) clear_flags(g, blockIdx.z);
+    u32* const spec = m.spec + ((size_t)prime << g.log_t) + blockIdx.x * G + c;
+    // Pass 1: levels 0-5 on rows 64 blk + k (bit-reversed spectrum in).
+    {
+        const u32* q = spec + ((u64)(blk * E) << log_c);
+        u32 x[1][E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) x[0][k] = __ldcs(q + ((u64)k << log_c));
+        dit_levels<A, 6, 1, 1, 2>(x, tw, pp.p);  // the row pass wrote [0, 2p) ([0, p) when wide)
+        u32* base = sm + c * VS + 65 * blk;
+#pragma unroll
+        for (int k = 0; k < E; ++k) base[k] = x[0][k];
+    }
+    __syncthreads();
+    // Pass 2: levels 6-11 on rows blk + 64k, canonical residues out.
+    {
+        const u32* base = sm + c * VS + blk;
+        u32 x[1][E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) x[0][k] = base[65 * k];
+        dit_levels<A, 6, E, 1>(x, pp.inv + blk, pp.p);
+        u32* q = spec + ((u64)blk << log_c);
+#pragma unroll
+        for (int k = 0; k < E; ++k) q[(u64)(k * E) << log_c] = A::canonical(x[0][k], pp.p);
+    }
+}
+
 // Rows per CTA of the row pass: enough that every thread owns a register block of
 // the first pass (2^(log_c - kMaxRB) blocks per row).
 __host__ __device__ constexpr int row_log_rpc(int log_c) {
@@ -515,7 +635,7 @@ __global__ void __launch_bounds__(256) k_step_tables(const __grid_constant__ Ste
     u64 n[4];
     step_table_sizes(b.log_t, b.log_r, n);
     const u64 mask = ((u64)1 << b.log_t) - 1;
-    const int log_rs = col_log_rs(b.log_r), log_sw = b.log_r - log_rs, log_nh = b.log_c - kRowTwLoBits;
+    const int log_rs = step_log_u(b.log_r), log_sw = b.log_r - log_rs, log_nh = b.log_c - kRowTwLoBits;
     const u64 total = n[0] + n[1] + n[2] + n[3];
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
         u64 k = i;
@@ -600,6 +720,10 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
         auto k = sign ? k_fwd_cols2<A, true> : k_fwd_cols2<A, false>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
         k<<<grid, kThreads, col2_smem(true), st>>>(g);
+    } else if constexpr (L == kCol4LogR) {
+        auto k = sign ? k_fwd_cols4<A, true> : k_fwd_cols4<A, false>;
+        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        k<<<grid, kCol4Threads, col4_smem(true), st>>>(g);
     } else {
         auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
@@ -627,6 +751,10 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
         auto k = k_inv_cols2<A>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
         return launch_dependent(k, grid, dim3(kThreads), col2_smem(false), st, g);
+    } else if constexpr (L == kCol4LogR) {
+        auto k = k_inv_cols4<A>;
+        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        return launch_dependent(k, grid, dim3(kCol4Threads), col4_smem(false), st, g);
     } else {
         auto k = k_inv_cols<A, L>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);

@@ -156,3 +156,29 @@ def test_fixed_lanes_capture_at_the_second_run(gpu, lanes):
     check_batch(gpu, torch, batch, shapes, torch.cuda.default_stream())
     assert batch.stats()["graph_replays"] == 2
     batch.close()
+
+
+def test_unbalanced_members_run_as_block_splits(gpu):
+    """Members that the planner splits (src/multiply/execute.rs:114-209 of the
+    reference) run as block splits inside the batch, beside ordinary classes, and
+    stay exact over repeated runs (the ordinary classes replay from a graph)."""
+    import torch
+
+    shapes = [Shape("mul", 1 << 20, 1000, 41, 42), Shape("mul", 1500, (1 << 20) + 7, 43, 44),
+              Shape("mul", 600000, 1000, 45, 46), Shape("mul", 5000, 4000, 47, 48), Shape("sqr", 3000, 3000, 49, 49),
+              Shape("conv", 3000, 2000, 50, 51, bits=16, signed=False)]
+    batch = gpu.GpuBatch()
+    reqs, keep = run_batch(gpu, torch, shapes)
+    want = [expected(s, a, b) for s, a, b, _ in keep]
+    for run in range(3):
+        for _, _, _, dst in keep:
+            dst.fill_(-1)
+        assert batch.run(reqs, torch.cuda.current_stream()), gpu.last_error()
+        torch.cuda.synchronize()
+        for (s, _, _, dst), w in zip(keep, want):
+            host = dst.cpu().numpy().view(np.uint64)
+            assert host[-1] == MASK, (run, s)
+            assert np.array_equal(host[:-1], w), (run, s)
+    assert batch.split_members == 9  # three split members per run
+    assert batch.status() == 0
+    batch.close()
