@@ -36,9 +36,8 @@ __host__ __device__ constexpr int col_group_log(int log_r) {
 }
 __host__ __device__ constexpr int col_log_rs(int log_r) { return 8 - col_group_log(log_r); }
 // Columns of 2^12 points (the wide lengths T = 2^24, 2^25) run as two radix-64
-// passes (k_fwd_cols4, k_inv_cols4 in transform.cu): 8 columns per CTA of 512
-// threads, 64 points per thread and pass.
-constexpr int kCol4LogR = 12, kCol4Threads = 512;
+// passes (k_fwd_cols4, k_inv_cols4 in transform.cu), 64 points per thread and pass.
+constexpr int kCol4LogR = 12;
 // log2 of the f4_a entries per column: the first factor of the forward four-step
 // twiddle of row r is indexed by the top log_u bits of brev(r), the second (f4_b)
 // by the rest.

@@ -86,7 +86,8 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     release_dependents();
     constexpr int B = M::SWEEPS < 8 ? M::SWEEPS : 8;  // sweeps per batch; B*RS is a multiple of 32
     static_assert(M::SWEEPS % B == 0 && (B * M::RS) % 32 == 0, "column batches");
-    const int prime = blockIdx.y;
+    const int prime = (int)(blockIdx.x % (u32)g.np);  // prime fastest: see k_fwd_cols4
+    const u32 group = blockIdx.x / (u32)g.np;
     // grid.z: operands (1 or 2) of one member, or per member in a batch (2, or 1
     // when the batch's other factor is a stored spectrum)
     const int op = g.batch ? (g.a_only ? 0 : blockIdx.z & 1) : blockIdx.z + g.op_base;
@@ -96,7 +97,7 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
     const int log_c = g.log_c;
-    const u32 col0 = (u32)(blockIdx.x << M::LOG_G);
+    const u32 col0 = group << M::LOG_G;
     const u32 col = col0 + M::col();
     const int r0 = M::row0();
     const u64 first = ((u64)r0 << log_c) + col;
@@ -193,7 +194,8 @@ __global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __
     extern __shared__ u32 sm[];
     release_dependents();
     constexpr int LOG_R = kCol2LogR, G = 8, VS = col_vstride(LOG_R), E = 32;
-    const int prime = blockIdx.y;
+    const int prime = (int)(blockIdx.x % (u32)g.np);  // prime fastest: see k_fwd_cols4
+    const u32 group = blockIdx.x / (u32)g.np;
     const int op = g.batch ? (g.a_only ? 0 : blockIdx.z & 1) : blockIdx.z + g.op_base;
     const Member m = member_of(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, false);
     if (op && m.square) return;
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
     const int log_c = g.log_c;
-    const u32 col0 = (u32)(blockIdx.x * G);
+    const u32 col0 = group * G;
     const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
     const u32 col = col0 + c;
     // f4_a rows of the CTA's columns, padded to 33 entries per column.
@@ -291,26 +293,39 @@ __global__ void __launch_bounds__(kThreads, NTT_INV_COLS2_MINB) k_inv_cols2(cons
 }
 
 // Column passes for R = 2^12 (the wide lengths T = 2^24 and 2^25) in two radix-64
-// passes, the k_fwd_cols2 design at twice the block: 8 columns per CTA, 512
-// threads, thread t owning column c = t mod 8 and either rows blk + 64k (pass 1)
+// passes, the k_fwd_cols2 design at twice the block: G columns per CTA of 64 G
+// threads, thread t owning column c = t mod G and either rows blk + 64k (pass 1)
 // or rows 64 blk + k (pass 2), k < 64. Row r = 64a + b sits at slot 65a + b of its
-// column, whose stride (4 mod 32) puts a warp's 8 columns x 4 blocks on 32
+// column, whose stride (32/G mod 32) puts a warp's G columns x 32/G blocks on 32
 // distinct banks in both orders. The forward four-step twiddle of row 64 blk + k is
 // w_T^(col * brev(row)) = f4_a[col][brev6(k)] * f4_b[col][brev6(blk)]. The level
 // roots of the consecutive-point pass (entries 1..63) sit in shared memory.
-constexpr int kCol4Vs = 65 * 64 + 4;
-static_assert(kCol4Vs % 32 == 4 && step_log_u(kCol4LogR) == 6, "radix-64 column layout");
+// G = 8 (512 threads of 128 registers, 135 KB) fills an SM with one CTA. G = 4
+// (two CTAs per SM, so that one CTA's loads overlap the other's butterflies)
+// measured slower on GB300 at T = 2^25: 1.58 against 1.20 ms forward, 0.76 against
+// 0.57 ms inverse (16-byte row segments instead of whole 32-byte sectors).
+#ifndef NTT_COLS4_LOG_G
+#define NTT_COLS4_LOG_G 3
+#endif
+constexpr int kCol4LogG = NTT_COLS4_LOG_G, kCol4G = 1 << kCol4LogG, kCol4Threads = 64 * kCol4G;
+constexpr int kCol4Vs = 65 * 64 + 32 / kCol4G;
+static_assert(kCol4Vs % 32 == 32 / kCol4G && step_log_u(kCol4LogR) == 6, "radix-64 column layout");
+static_assert(kCol4Threads * 128 * (kCol4LogG == 2 ? 2 : 1) <= 65536, "register budget of the column CTAs");
 
 static size_t col4_smem(bool fwd) {
-    return (size_t)8 * kCol4Vs * sizeof(u32) + 64 * sizeof(uint2) + (fwd ? 8 * 65 * sizeof(uint2) : 0);
+    return (size_t)kCol4G * kCol4Vs * sizeof(u32) + 64 * sizeof(uint2) + (fwd ? kCol4G * 65 * sizeof(uint2) : 0);
 }
 
 template <class A, bool SIGNED>
-__global__ void __launch_bounds__(kCol4Threads, 1) k_fwd_cols4(const __grid_constant__ TransformArgs g) {
+__global__ void __launch_bounds__(kCol4Threads, kCol4LogG == 2 ? 2 : 1)
+    k_fwd_cols4(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     release_dependents();
-    constexpr int G = 8, VS = kCol4Vs, E = 64;
-    const int prime = blockIdx.y;
+    constexpr int G = kCol4G, LOG_G = kCol4LogG, VS = kCol4Vs, E = 64;
+    // grid.x runs over (column group, prime) with the prime fastest, so the np CTAs
+    // that read the same limbs run together and all but the first read them from L2
+    const int prime = (int)(blockIdx.x % (u32)g.np);
+    const u32 group = blockIdx.x / (u32)g.np;
     const int op = g.batch ? (g.a_only ? 0 : blockIdx.z & 1) : blockIdx.z + g.op_base;
     const Member m = member_of(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, false);
     if (op && m.square) return;
@@ -318,8 +333,8 @@ __global__ void __launch_bounds__(kCol4Threads, 1) k_fwd_cols4(const __grid_cons
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
     const int log_c = g.log_c;
-    const u32 col0 = (u32)(blockIdx.x * G);
-    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    const u32 col0 = group * G;
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> LOG_G;
     const u32 col = col0 + c;
     uint2* tw = reinterpret_cast<uint2*>(sm + G * VS);
     uint2* fa = tw + 64;  // f4_a rows of the CTA's columns, 65 entries apart
@@ -368,15 +383,16 @@ __global__ void __launch_bounds__(kCol4Threads, 1) k_fwd_cols4(const __grid_cons
 }
 
 template <class A>
-__global__ void __launch_bounds__(kCol4Threads, 1) k_inv_cols4(const __grid_constant__ TransformArgs g) {
+__global__ void __launch_bounds__(kCol4Threads, kCol4LogG == 2 ? 2 : 1)
+    k_inv_cols4(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
-    constexpr int G = 8, VS = kCol4Vs, E = 64;
+    constexpr int G = kCol4G, LOG_G = kCol4LogG, VS = kCol4Vs, E = 64;
     const int prime = blockIdx.y;
     const PrimeParams& pp = g.ps.pr[prime];
     const Member m = member_of(g, blockIdx.z, false);
     release_dependents();
     const int log_c = g.log_c;
-    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> LOG_G;
     uint2* tw = reinterpret_cast<uint2*>(sm + G * VS);
     if (threadIdx.x < 64) tw[threadIdx.x] = __ldg(pp.inv + threadIdx.x);
     __syncthreads();
@@ -715,7 +731,8 @@ static size_t col2_smem(bool fwd) {
 template <class A, int L>
 static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     const unsigned ops = g.op_count ? g.op_count : (square ? 1 : 2);
-    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? (g.a_only ? 1 : 2) * g.count : ops);
+    const unsigned zdim = g.batch ? (g.a_only ? 1 : 2) * g.count : ops;
+    const dim3 grid((1u << (g.log_c - col_group_log(L))) * (unsigned)g.np, 1, zdim);
     if constexpr (L == kCol2LogR) {
         auto k = sign ? k_fwd_cols2<A, true> : k_fwd_cols2<A, false>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
@@ -723,7 +740,7 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
     } else if constexpr (L == kCol4LogR) {
         auto k = sign ? k_fwd_cols4<A, true> : k_fwd_cols4<A, false>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
-        k<<<grid, kCol4Threads, col4_smem(true), st>>>(g);
+        k<<<dim3((1u << (g.log_c - kCol4LogG)) * (unsigned)g.np, 1, zdim), kCol4Threads, col4_smem(true), st>>>(g);
     } else {
         auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
@@ -746,7 +763,8 @@ static cudaError_t rows_at(const TransformArgs& g, int mode, cudaStream_t st, bo
 
 template <class A, int L>
 static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool init) {
-    const dim3 grid(1u << (g.log_c - col_group_log(L)), g.np, g.batch ? g.count : 1);
+    const int log_g = L == kCol4LogR ? kCol4LogG : col_group_log(L);
+    const dim3 grid(1u << (g.log_c - log_g), g.np, g.batch ? g.count : 1);
     if constexpr (L == kCol2LogR) {
         auto k = k_inv_cols2<A>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
