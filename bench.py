@@ -147,20 +147,34 @@ def operand_sets(count: int):
     return [(operand(LA, 1 + 2 * i), operand(LB, 2 + 2 * i)) for i in range(count)]
 
 
-def cpu_sample(threads: int, seconds: float = 12.0, max_products: int = 20) -> dict:
-    """Times the oracle on whole products until `seconds` elapse (bounded sample)."""
+def cpu_sample(threads: int, seconds: float = 12.0, max_products: int = 20, min_products: int = 5) -> dict:
+    """Times the oracle on whole products (bounded sample): at least `min_products`
+    after one warm-up product, then more until `seconds` elapse; the value is the
+    median per-product time. A single-threaded sample runs pinned to one core."""
+    import statistics
+
     import oracle
 
     from nttanafis_gb300.operands import operand
 
     a, b = operand(LA, 1), operand(LB, 2)
-    oracle.mul(a, b, threads)  # tables, page-in
-    done, t0 = 0, time.perf_counter()
-    while done < max_products and (time.perf_counter() - t0 < seconds or done == 0):
-        oracle.mul(a, b, threads)
-        done += 1
-    dt = time.perf_counter() - t0
-    return {"value": done / dt, "seconds_per_product": dt / done, "products": done, "threads": threads}
+    pinned = None
+    if threads == 1 and hasattr(os, "sched_getaffinity"):
+        pinned = os.sched_getaffinity(0)
+        os.sched_setaffinity(0, {min(pinned)})
+    try:
+        oracle.mul(a, b, threads)  # tables, page-in
+        times, t0 = [], time.perf_counter()
+        while len(times) < max_products and (len(times) < min_products or time.perf_counter() - t0 < seconds):
+            t = time.perf_counter()
+            oracle.mul(a, b, threads)
+            times.append(time.perf_counter() - t)
+    finally:
+        if pinned is not None:
+            os.sched_setaffinity(0, pinned)
+    med = statistics.median(times)
+    return {"value": 1.0 / med, "seconds_per_product": med, "products": len(times), "threads": threads,
+            "pinned_core": min(pinned) if pinned is not None else None}
 
 
 def cpu_model() -> str:
@@ -736,12 +750,15 @@ def run_gpu(args) -> None:
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
         multi = cpu_sample(cores, seconds=args.cpu_seconds)
-        single = cpu_sample(1, seconds=args.cpu_seconds / 2, max_products=3)
+        single = cpu_sample(1, seconds=args.cpu_seconds / 2, max_products=10)
         line["cpu_baseline"] = {
             "value": multi["value"], "unit": "products/s", "cores": cores, "kind": "port",
-            "sample": (f"{multi['products']} whole 1M x 1M products on {cores} threads ({cpu_model()}); "
-                       f"single thread: {single['value']:.3f} products/s over {single['products']}"),
+            "sample": (f"median of {multi['products']} whole 1M x 1M products on {cores} threads ({cpu_model()}); "
+                       f"single thread pinned to core {single['pinned_core']}: {single['value']:.3f} products/s, "
+                       f"median of {single['products']}"),
             "single_thread_value": single["value"],
+            "single_thread_ms": 1000.0 * single["seconds_per_product"],
+            "published_reference_single_core_ms": 43.4,
         }
     if rank == 0:
         print(json.dumps(line), flush=True)
