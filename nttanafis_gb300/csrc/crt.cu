@@ -254,13 +254,12 @@ __device__ __forceinline__ bool admitted(const u32* __restrict__ votes) {
     return !__syncthreads_or(bad);
 }
 
-// Admission scan (src/convolve.rs:169-184) for the convolutions whose transform
-// does not load every coefficient in one CTA: CTA s of a convolution reads every
+// Admission scan (src/convolve.rs:169-184) for the schoolbook convolutions, which
+// have no transform to check the coefficients as it loads them: CTA s reads every
 // (kAdmitSlots)-th stretch of a and b, compares each coefficient with its bound
 // (the magnitude of a two's complement coefficient when signed) and writes vote s.
 // Each thread keeps kAdmitUnroll loads in flight, so that the scan runs near the
-// HBM rate. grid = (kAdmitSlots, members); a single convolution passes its
-// arguments, a batch class its descriptors.
+// HBM rate. grid = kAdmitSlots.
 constexpr int kAdmitThreads = 1024, kAdmitUnroll = 8;
 
 template <bool SIGNED>
@@ -282,18 +281,7 @@ __device__ __forceinline__ int scan_over(const u64* __restrict__ v, u64 n, u64 m
 template <bool SIGNED>
 __global__ void __launch_bounds__(kAdmitThreads) k_conv_admit(const u64* __restrict__ a, u64 la,
                                                               const u64* __restrict__ b, u64 lb, u64 max_a,
-                                                              u64 max_b, u32* __restrict__ votes,
-                                                              const ProductDesc* __restrict__ batch) {
-    if (batch) {
-        const ProductDesc& d = batch[blockIdx.y];
-        a = d.a;
-        b = d.b;
-        la = d.la;
-        lb = d.lb;
-        max_a = d.max_a;
-        max_b = d.max_b;
-        votes = d.votes;
-    }
+                                                              u64 max_b, u32* __restrict__ votes) {
     int bad = scan_over<SIGNED>(a, la, max_a);
     if (b != a || lb != la || max_b != max_a) bad |= scan_over<SIGNED>(b, lb, max_b);
     bad = __syncthreads_or(bad);
@@ -436,16 +424,21 @@ cudaError_t launch_crt_conv(const u32* resid, int log_t, u64 conv_len, u64* dst,
 cudaError_t launch_conv_admit(const u64* a, u64 la, const u64* b, u64 lb, u64 max_a, u64 max_b, bool sign,
                               u32* votes, cudaStream_t st) {
     if (sign)
-        k_conv_admit<true><<<kAdmitSlots, kAdmitThreads, 0, st>>>(a, la, b, lb, max_a, max_b, votes, nullptr);
+        k_conv_admit<true><<<kAdmitSlots, kAdmitThreads, 0, st>>>(a, la, b, lb, max_a, max_b, votes);
     else
-        k_conv_admit<false><<<kAdmitSlots, kAdmitThreads, 0, st>>>(a, la, b, lb, max_a, max_b, votes, nullptr);
+        k_conv_admit<false><<<kAdmitSlots, kAdmitThreads, 0, st>>>(a, la, b, lb, max_a, max_b, votes);
     return cudaGetLastError();
 }
 
-cudaError_t launch_conv_admit_batch(const ProductDesc* batch, int count, bool sign, cudaStream_t st) {
-    const dim3 grid(kAdmitSlots, count);
-    if (sign) k_conv_admit<true><<<grid, kAdmitThreads, 0, st>>>(nullptr, 0, nullptr, 0, 0, 0, nullptr, batch);
-    else k_conv_admit<false><<<grid, kAdmitThreads, 0, st>>>(nullptr, 0, nullptr, 0, 0, 0, nullptr, batch);
+// Zeroes the admission votes of every convolution member of a batch class, before
+// a forward column pass that raises them. grid = members.
+__global__ void __launch_bounds__(kAdmitSlots) k_clear_votes(const ProductDesc* __restrict__ batch) {
+    u32* votes = batch[blockIdx.x].votes;
+    if (votes) votes[threadIdx.x] = 0u;
+}
+
+cudaError_t launch_clear_votes_batch(const ProductDesc* batch, int count, cudaStream_t st) {
+    k_clear_votes<<<count, kAdmitSlots, 0, st>>>(batch);
     return cudaGetLastError();
 }
 

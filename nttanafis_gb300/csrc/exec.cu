@@ -30,11 +30,12 @@ bool run_members(const ProductDesc* descs, int n, const Geom& g0, bool sq, u64 m
     const bool sign = g0.sign != 0;
     mark(st);
     // coefficient bounds of every convolution member (its votes): checked by the
-    // one-CTA transform as it loads them, or else by a scan kernel first
+    // one-CTA transform or the forward column pass as they load the coefficients;
+    // the column pass only raises votes, so they are zeroed first
     ta.admit = g0.conv ? 1 : 0;
     if (g0.conv && g0.log_t > kMaxBlockLog) {
         note_launches(1);
-        if (!cuda_ok(launch_conv_admit_batch(descs, n, sign, st), "batched admission launch")) return false;
+        if (!cuda_ok(launch_clear_votes_batch(descs, n, st), "batched vote clearing launch")) return false;
         mark(st);
     }
     if (!shared_spec && !g0.conv && g0.log_t <= kFusedMaxLog && g0.np == kFusedPrimes && !g0.wide) {
@@ -163,10 +164,14 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
         return ok;
     }
     // Device-side admission of a convolution's coefficients: votes at the start of
-    // the scratch, written by the one-CTA transform as it loads the coefficients,
-    // or else by a scan kernel first.
+    // the scratch, written by the transform that loads the coefficients (the
+    // one-CTA transform writes every vote; the forward column pass only raises
+    // them, so they are zeroed first), or by a scan kernel before the schoolbook.
     u32* votes = g.conv && admit ? (u32*)scratch : nullptr;
-    if (votes && (g.schoolbook || single_log_r(g) != 0)) {
+    if (votes && !g.schoolbook && single_log_r(g) != 0 &&
+        !cuda_ok(cudaMemsetAsync(votes, 0, kAdmitBytes, st), "zero admission votes"))
+        return false;
+    if (votes && g.schoolbook) {
         if (b_ready && !cuda_ok(cudaStreamWaitEvent(st, b_ready, 0), "cudaStreamWaitEvent")) return false;
         b_ready = nullptr;
         note_launches(1);
@@ -226,6 +231,9 @@ bool execute(const Geom& g, bool square, const u64* d_a, const u64* d_b, u64* d_
     } else {
         ta.log_r = log_r;
         ta.log_c = g.log_t - ta.log_r;
+        ta.votes = votes;
+        ta.max_a = g.max_a;
+        ta.max_b = square ? g.max_a : g.max_b;
         if (b_ready && !square) {
             note_launches(1);
             ta.op_count = 1;

@@ -92,8 +92,9 @@ struct TransformArgs {
     u32 flag_words;
     u64* dst;          // product limbs of the fused one-kernel path (single member)
     u64 out_len;
-    // Coefficient admission of a convolution by the one-CTA transform (the prime-0
-    // CTA checks the coefficients it loads and writes the votes): votes (null: no
+    // Coefficient admission of a convolution by the transform that loads the
+    // coefficients (prime 0's CTAs check them: the one-CTA transform writes every
+    // vote, the forward column pass raises votes zeroed before it): votes (null: no
     // check) and bounds; batch members take theirs from the descriptors.
     u32* votes;
     u64 max_a, max_b;
@@ -188,11 +189,12 @@ cudaError_t launch_crt_mul_batch(const ProductDesc* batch, int count, int max_ti
                                  const CrtParams& cp, cudaStream_t st, u32* status = nullptr);
 cudaError_t launch_crt_conv_batch(const ProductDesc* batch, int count, u64 max_conv_len, int log_t,
                                   const CrtParams& cp, cudaStream_t st, u32* status = nullptr);
-// Admission votes of one convolution (votes: kAdmitSlots u32), or of every member
-// of a batch class (into each member's votes).
+// Admission votes of one schoolbook convolution (votes: kAdmitSlots u32, every one
+// written), and the zeroing of a batch class's member votes before a forward column
+// pass that raises them.
 cudaError_t launch_conv_admit(const u64* a, u64 la, const u64* b, u64 lb, u64 max_a, u64 max_b, bool sign,
                               u32* votes, cudaStream_t st);
-cudaError_t launch_conv_admit_batch(const ProductDesc* batch, int count, bool sign, cudaStream_t st);
+cudaError_t launch_clear_votes_batch(const ProductDesc* batch, int count, cudaStream_t st);
 // dst[0, len) += add[0, len) with carries (flags: carry_flag_words(len), zeroed).
 cudaError_t launch_add_limbs(u64* dst, const u64* add, u64 len, u32* flags, cudaStream_t st,
                              u32* status = nullptr);

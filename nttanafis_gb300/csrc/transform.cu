@@ -79,7 +79,9 @@ struct ColumnMap {
     }
 };
 
-template <class A, bool SIGNED, int LOG_R>
+// CHECK: a convolution's coefficients are checked against their bounds on the way
+// in (column_votes); products are instantiated without the check.
+template <class A, bool SIGNED, int LOG_R, bool CHECK = SIGNED>
 __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     using M = ColumnMap<LOG_R>;
@@ -96,6 +98,10 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
     const PrimeParams& pp = g.ps.pr[prime];
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
+    u64 vmax = 0;
+    u32* const votes =
+        CHECK ? column_votes(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, op, prime, vmax) : nullptr;
+    int bad = 0;
     const int log_c = g.log_c;
     const u32 col0 = group << M::LOG_G;
     const u32 col = col0 + M::col();
@@ -133,14 +139,18 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
 #pragma unroll
                 for (int k = 0; k < E / 2; ++k) {
                     const u64 n = n0 + k * kstep;
-                    x[0][k] = n < len ? reduce_coefficient<A, SIGNED>(__ldcs(src + n), pp) : 0u;
+                    const u64 v = n < len ? __ldcs(src + n) : 0;
+                    if (CHECK && votes) bad |= coefficient_over<SIGNED>(v, vmax);
+                    x[0][k] = n < len ? reduce_coefficient<A, SIGNED>(v, pp) : 0u;
                 }
                 dif_levels<A, RB, HQ, 1, true>(x, pp.fwd + gg, pp.p);
             } else {
 #pragma unroll
                 for (int k = 0; k < E; ++k) {
                     const u64 n = n0 + k * kstep;
-                    x[0][k] = n < len ? reduce_coefficient<A, SIGNED>(__ldcs(src + n), pp) : 0u;
+                    const u64 v = n < len ? __ldcs(src + n) : 0;
+                    if (CHECK && votes) bad |= coefficient_over<SIGNED>(v, vmax);
+                    x[0][k] = n < len ? reduce_coefficient<A, SIGNED>(v, pp) : 0u;
                 }
                 dif_levels<A, RB, HQ, 1>(x, pp.fwd + gg, pp.p);
             }
@@ -149,6 +159,7 @@ __global__ void NTT_COLS_BOUNDS k_fwd_cols(const __grid_constant__ TransformArgs
             for (int k = 0; k < E; ++k) base[slot_offset<HQ>(k)] = x[0][k];
         }
     }
+    if (CHECK && bad) votes[(blockIdx.x + threadIdx.x) % kAdmitSlots] = 1u;
     __syncthreads();
     dif_full<A, LOG_R, kThreads, M::G, M::VS, kMaxRB>(sm, tw, pp.p);
     // Four-step twiddle w_T^(col * brev(row)) = fa * fb[col][brev(k)], then the store.
@@ -189,7 +200,7 @@ static_assert(col_group_log(10) == 3 && col_log_rs(10) == 5, "two-pass columns a
 #define NTT_INV_COLS2_MINB 4
 #endif
 
-template <class A, bool SIGNED>
+template <class A, bool SIGNED, bool CHECK = SIGNED>
 __global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
     release_dependents();
@@ -202,6 +213,10 @@ __global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __
     const PrimeParams& pp = g.ps.pr[prime];
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
+    u64 vmax = 0;
+    u32* const votes =
+        CHECK ? column_votes(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, op, prime, vmax) : nullptr;
+    int bad = 0;
     const int log_c = g.log_c;
     const u32 col0 = group * G;
     const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> 3;
@@ -218,19 +233,26 @@ __global__ void __launch_bounds__(kThreads, NTT_COLS2_MINB) k_fwd_cols2(const __
         u32 x[1][E];
         if (half) {
 #pragma unroll
-            for (int k = 0; k < E / 2; ++k)
-                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            for (int k = 0; k < E / 2; ++k) {
+                const u64 v = n0 + k * kstep < len ? __ldcs(p0 + k * kstep) : 0;
+                if (CHECK && votes) bad |= coefficient_over<SIGNED>(v, vmax);
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(v, pp) : 0u;
+            }
             dif_levels<A, 5, E, 1, true>(x, pp.fwd + blk, pp.p);
         } else {
 #pragma unroll
-            for (int k = 0; k < E; ++k)
-                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            for (int k = 0; k < E; ++k) {
+                const u64 v = n0 + k * kstep < len ? __ldcs(p0 + k * kstep) : 0;
+                if (CHECK && votes) bad |= coefficient_over<SIGNED>(v, vmax);
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(v, pp) : 0u;
+            }
             dif_levels<A, 5, E, 1>(x, pp.fwd + blk, pp.p);
         }
         u32* base = sm + c * VS + blk;
 #pragma unroll
         for (int k = 0; k < E; ++k) base[33 * k] = x[0][k];
     }
+    if (CHECK && bad) votes[(blockIdx.x + threadIdx.x) % kAdmitSlots] = 1u;
     __syncthreads();
     // Pass 2: levels 5-9 on rows 32 blk + k, four-step twiddle, store.
     {
@@ -316,7 +338,7 @@ static size_t col4_smem(bool fwd) {
     return (size_t)kCol4G * kCol4Vs * sizeof(u32) + 64 * sizeof(uint2) + (fwd ? kCol4G * 65 * sizeof(uint2) : 0);
 }
 
-template <class A, bool SIGNED>
+template <class A, bool SIGNED, bool CHECK = SIGNED>
 __global__ void __launch_bounds__(kCol4Threads, kCol4LogG == 2 ? 2 : 1)
     k_fwd_cols4(const __grid_constant__ TransformArgs g) {
     extern __shared__ u32 sm[];
@@ -332,6 +354,10 @@ __global__ void __launch_bounds__(kCol4Threads, kCol4LogG == 2 ? 2 : 1)
     const PrimeParams& pp = g.ps.pr[prime];
     const u64* __restrict__ src = op ? m.b : m.a;
     const u64 len = op ? m.lb : m.la;
+    u64 vmax = 0;
+    u32* const votes =
+        CHECK ? column_votes(g, g.batch ? (g.a_only ? blockIdx.z : blockIdx.z >> 1) : 0, op, prime, vmax) : nullptr;
+    int bad = 0;
     const int log_c = g.log_c;
     const u32 col0 = group * G;
     const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> LOG_G;
@@ -349,19 +375,26 @@ __global__ void __launch_bounds__(kCol4Threads, kCol4LogG == 2 ? 2 : 1)
         u32 x[1][E];
         if (half) {
 #pragma unroll
-            for (int k = 0; k < E / 2; ++k)
-                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            for (int k = 0; k < E / 2; ++k) {
+                const u64 v = n0 + k * kstep < len ? __ldcs(p0 + k * kstep) : 0;
+                if (CHECK && votes) bad |= coefficient_over<SIGNED>(v, vmax);
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(v, pp) : 0u;
+            }
             dif_levels<A, 6, E, 1, true>(x, pp.fwd + blk, pp.p);
         } else {
 #pragma unroll
-            for (int k = 0; k < E; ++k)
-                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(__ldcs(p0 + k * kstep), pp) : 0u;
+            for (int k = 0; k < E; ++k) {
+                const u64 v = n0 + k * kstep < len ? __ldcs(p0 + k * kstep) : 0;
+                if (CHECK && votes) bad |= coefficient_over<SIGNED>(v, vmax);
+                x[0][k] = n0 + k * kstep < len ? reduce_coefficient<A, SIGNED>(v, pp) : 0u;
+            }
             dif_levels<A, 6, E, 1>(x, pp.fwd + blk, pp.p);
         }
         u32* base = sm + c * VS + blk;
 #pragma unroll
         for (int k = 0; k < E; ++k) base[65 * k] = x[0][k];
     }
+    if (CHECK && bad) votes[(blockIdx.x + threadIdx.x) % kAdmitSlots] = 1u;
     __syncthreads();
     // Pass 2: levels 6-11 on rows 64 blk + k, four-step twiddle, store.
     {
@@ -733,17 +766,29 @@ static cudaError_t fwd_cols_at(const TransformArgs& g, bool square, bool sign, c
     const unsigned ops = g.op_count ? g.op_count : (square ? 1 : 2);
     const unsigned zdim = g.batch ? (g.a_only ? 1 : 2) * g.count : ops;
     const dim3 grid((1u << (g.log_c - col_group_log(L))) * (unsigned)g.np, 1, zdim);
+    // unsigned convolutions take the checking instantiation when they carry votes;
+    // signed ones always do (a product is never signed)
+    const bool check = g.batch ? g.admit != 0 : g.votes != nullptr;
     if constexpr (L == kCol2LogR) {
-        auto k = sign ? k_fwd_cols2<A, true> : k_fwd_cols2<A, false>;
-        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        auto k = sign ? k_fwd_cols2<A, true> : check ? k_fwd_cols2<A, false, true> : k_fwd_cols2<A, false>;
+        if (init) {
+            cudaError_t e = opt_in(k_fwd_cols2<A, false, true>, NTT_COLS_CARVEOUT);
+            return e == cudaSuccess ? opt_in(k, NTT_COLS_CARVEOUT) : e;
+        }
         k<<<grid, kThreads, col2_smem(true), st>>>(g);
     } else if constexpr (L == kCol4LogR) {
-        auto k = sign ? k_fwd_cols4<A, true> : k_fwd_cols4<A, false>;
-        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        auto k = sign ? k_fwd_cols4<A, true> : check ? k_fwd_cols4<A, false, true> : k_fwd_cols4<A, false>;
+        if (init) {
+            cudaError_t e = opt_in(k_fwd_cols4<A, false, true>, NTT_COLS_CARVEOUT);
+            return e == cudaSuccess ? opt_in(k, NTT_COLS_CARVEOUT) : e;
+        }
         k<<<dim3((1u << (g.log_c - kCol4LogG)) * (unsigned)g.np, 1, zdim), kCol4Threads, col4_smem(true), st>>>(g);
     } else {
-        auto k = sign ? k_fwd_cols<A, true, L> : k_fwd_cols<A, false, L>;
-        if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+        auto k = sign ? k_fwd_cols<A, true, L> : check ? k_fwd_cols<A, false, L, true> : k_fwd_cols<A, false, L>;
+        if (init) {
+            cudaError_t e = opt_in(k_fwd_cols<A, false, L, true>, NTT_COLS_CARVEOUT);
+            return e == cudaSuccess ? opt_in(k, NTT_COLS_CARVEOUT) : e;
+        }
         k<<<grid, kThreads, col_smem(L, true), st>>>(g);
     }
     return cudaGetLastError();

@@ -43,6 +43,25 @@ __device__ __forceinline__ Member member_of(const TransformArgs& g, int idx, boo
     return Member{g.a, g.b, g.la, g.lb, g.spec, g.conv_len, square};
 }
 
+// Admission votes of a convolution (src/convolve.rs:169-184) checked by the forward
+// column passes as they load the coefficients: the votes and bound of operand op
+// of a member, or null when the CTA checks nothing. Only prime 0's CTAs check, as
+// every prime reads the same coefficients. The votes were zeroed before the pass; a
+// thread that loads a coefficient above its bound sets one (the CRT kernel then
+// leaves the destination unwritten).
+__device__ __forceinline__ u32* column_votes(const TransformArgs& g, int member, int op, int prime, u64& mx) {
+    mx = 0;
+    if (prime != 0) return nullptr;
+    if (g.batch) {
+        if (!g.admit) return nullptr;
+        const ProductDesc& d = g.batch[member];
+        mx = op ? d.max_b : d.max_a;
+        return d.votes;
+    }
+    mx = op ? g.max_b : g.max_a;
+    return g.votes;
+}
+
 // Clears the CRT look-back flags of a member (products only; see k_crt_mul).
 __device__ __forceinline__ void clear_flags(const TransformArgs& g, int idx) {
     u32* f = g.flags;

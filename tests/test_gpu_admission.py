@@ -120,3 +120,30 @@ def test_batch_member_over_bound_is_left_unwritten(gpu):
     assert np.array_equal(host(mul_dst), oracle.mul(mul_a, mul_b))
     assert batch.status() == 0
     batch.close()
+
+
+@pytest.mark.parametrize("la,lb,mx,signed", [(1 << 20, (1 << 20) - 5, 0xFFFF, False), (1 << 20, 3000, (1 << 31) - 1, True),
+                                             (1 << 23, (1 << 23) - 3, 0xFFFF, False)])
+def test_column_pass_admission_at_large_sizes(gpu, la, lb, mx, signed):
+    # the two-pass 2^10-point column kernel (T = 2^21) and the radix-64 2^12-point
+    # one (T = 2^24, wide primes) check the coefficients as they load them
+    import torch
+
+    stream = torch.cuda.current_stream()
+    w = gpu.GpuConvWorkspace()
+    plan = gpu.ConvPlan.new(la, lb, mx, mx, signed)
+    assert w.prepare(plan)
+    a, b = operands(la, lb, mx, signed, 701)
+    for bad_a, bad_b in [(over_bound(a, mx, signed, la - 1), b), (a, over_bound(b, mx, signed, lb // 3))]:
+        dst = torch.full((plan.output_len(),), -1, dtype=torch.int64, device="cuda")
+        assert w.convolve_device(dst, dev(torch, bad_a), dev(torch, bad_b), stream)
+        torch.cuda.synchronize()
+        assert w.status() == gpu.STATUS_BOUND
+        assert bool((dst == -1).all()), "a rejected convolution wrote its destination"
+    dst = torch.full((plan.output_len(),), -1, dtype=torch.int64, device="cuda")
+    assert w.convolve_device(dst, dev(torch, a), dev(torch, b), stream)
+    torch.cuda.synchronize()
+    assert w.status() == 0
+    if la <= 1 << 20:
+        assert np.array_equal(host(dst), oracle.conv(a, b, mx, mx, signed, THREADS))
+    w.close()

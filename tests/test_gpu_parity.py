@@ -245,6 +245,36 @@ def test_wide_prime_class_2_pow_24(ws):
     assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
 
 
+def test_wide_block_split(ws):
+    # blocks of 2^24-point transforms (wide primes) sharing the shorter operand's
+    # spectrum: the 2^12-point column kernels in their one-operand spectrum mode
+    a, b = operand(40_000_000, 33), operand(2_000_000, 34)
+    assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
+    assert fingerprint_ok(a, b, gpu_mul(ws, b, a))
+
+
+def test_wide_class_in_a_batch(gpu):
+    # a T = 2^24 member beside a short one: the 2^12-point column kernels in batch mode
+    import torch
+
+    big_a, big_b = operand(1 << 23, 35), operand((1 << 23) - 7, 36)
+    small_a, small_b = operand(3000, 37), operand(2000, 38)
+    batch = gpu.GpuBatch()
+    dev = [torch.from_numpy(x.view(np.int64)).cuda() for x in (big_a, big_b, small_a, small_b)]
+    d_big = torch.full((big_a.size + big_b.size + 1,), -1, dtype=torch.int64, device="cuda")
+    d_small = torch.full((small_a.size + small_b.size + 1,), -1, dtype=torch.int64, device="cuda")
+    reqs = [gpu.Request(d_big, dev[0], dev[1]), gpu.Request(d_small, dev[2], dev[3])]
+    assert batch.run(reqs, torch.cuda.current_stream()), gpu.last_error()
+    torch.cuda.synchronize()
+    big = d_big.cpu().numpy().view(np.uint64)
+    small = d_small.cpu().numpy().view(np.uint64)
+    assert big[-1] == MASK and small[-1] == MASK
+    assert fingerprint_ok(big_a, big_b, big[:-1])
+    assert np.array_equal(small[:-1], oracle.mul(small_a, small_b, THREADS))
+    assert batch.status() == 0
+    batch.close()
+
+
 def test_config_16m_mul_and_sqr_exact(ws, golden):
     # bit-exact against the oracle's digests (tests/golden/make_big_digests.py),
     # with the Mersenne fingerprints as a second, independent check
