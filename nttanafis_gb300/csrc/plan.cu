@@ -71,9 +71,9 @@ static u32 generator(u32 p) {
     return 0;
 }
 
-static std::vector<u32> primes_for(int log_t) {
+static std::vector<u32> primes_for(int log_t, bool wide) {
     std::vector<u32> out;
-    if (log_t <= kLazyMaxLog) {
+    if (!wide) {
         for (u32 p : kLazyPrimes) if (valuation(p) >= log_t) out.push_back(p);
     } else {
         for (u32 p : kWidePrimes) if (valuation(p) >= log_t) out.push_back(p);
@@ -121,19 +121,52 @@ static int ceil_log2(u64 x) { return x <= 1 ? 0 : 64 - __builtin_clzll(x - 1); }
 // Plans
 
 
-static bool choose_primes(Geom& g, int need_bits) {
-    const std::vector<u32> cand = primes_for(g.log_t);
+// Fewest primes of one class whose capacity holds need_bits (0: none does).
+static int fewest_primes(const std::vector<u32>& cand, int need_bits, int& cap) {
     for (int np = 1; np <= (int)cand.size(); ++np) {
-        const int cap = capacity(cand, np);
-        if (cap >= need_bits) {
-            g.np = np;
-            g.cap = cap;
-            for (int i = 0; i < np; ++i) g.primes[i] = cand[i];
-            g.wide = g.log_t > kLazyMaxLog;
-            return true;
+        cap = capacity(cand, np);
+        if (cap >= need_bits) return np;
+    }
+    return 0;
+}
+
+// Lengths up to 2^23 take the lazy primes (p < 2^30), longer ones the wide primes
+// (p < 2^31, canonical arithmetic). At 2^22 and 2^23 the wide primes are taken as
+// well when they hold the coefficients with one prime fewer: five lazy primes hold
+// 148 and 147 bits there, five wide ones 153, so a product whose shorter operand
+// has more than 2^20 (2^19) limbs needs six lazy primes but five wide ones. The
+// wide butterfly costs the same per point (one more ALU subtraction, off the
+// multiplier pipe), so a prime fewer is a sixth less work. Those lengths run the
+// two-pass 2^10-point column kernels and the 2^12- and 2^13-point rows.
+constexpr int kWideFromLog = 22;
+
+static bool choose_primes(Geom& g, int need_bits) {
+    const bool lazy_ok = g.log_t <= kLazyMaxLog;
+    const bool wide_ok = g.log_t >= kWideFromLog;
+    std::vector<u32> cand;
+    int cap = 0, np = 0;
+    bool wide = false;
+    if (lazy_ok) {
+        cand = primes_for(g.log_t, false);
+        np = fewest_primes(cand, need_bits, cap);
+    }
+    if (wide_ok) {
+        int wcap = 0;
+        const std::vector<u32> wcand = primes_for(g.log_t, true);
+        const int wnp = fewest_primes(wcand, need_bits, wcap);
+        if (wnp && (!np || wnp < np)) {
+            cand = wcand;
+            np = wnp;
+            cap = wcap;
+            wide = true;
         }
     }
-    return false;
+    if (!np) return false;
+    g.np = np;
+    g.cap = cap;
+    for (int i = 0; i < np; ++i) g.primes[i] = cand[i];
+    g.wide = wide ? 1 : 0;
+    return true;
 }
 
 // Longest operand of a split product (limbs).
@@ -430,7 +463,9 @@ bool split_range(int log_t, int& lo, int& hi) {
 
 int four_step_log_r(const Geom& g) {
     if (g.log_t <= kMaxBlockLog) return 0;
-    const int o = g.wide ? 0 : g_split[g.log_t].load(std::memory_order_relaxed);
+    // wide: 2^12-point columns from 2^24 on, 2^10-point ones at 2^22 and 2^23
+    if (g.wide) return g.log_t >= 24 ? 12 : 10;
+    const int o = g_split[g.log_t].load(std::memory_order_relaxed);
     return o ? o : g.log_t / 2;
 }
 
@@ -441,13 +476,14 @@ int single_log_r(const Geom& g) {
 
 // Fills the kernel constants of a plan whose four-step split is R = 2^log_r (0 for
 // the one-CTA lengths); builds missing tables on the current device.
-static std::map<std::tuple<int, int, int, int>, std::pair<PrimeSet, CrtParams>> g_param_cache;
+static std::map<std::tuple<int, int, int, int, int>, std::pair<PrimeSet, CrtParams>> g_param_cache;
 
 bool prepare_params(const Geom& g, int log_r, PrimeSet& ps, CrtParams& cp) {
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
     std::lock_guard<std::mutex> lock(g_table_mutex);
-    const auto key = std::make_tuple(dev, g.log_t, g.np, log_r);
+    // the prime set is fixed by the length, the prime count and the class
+    const auto key = std::make_tuple(dev, g.log_t, g.np, log_r, g.wide);
     auto hit = g_param_cache.find(key);
     if (hit != g_param_cache.end()) {
         ps = hit->second.first;

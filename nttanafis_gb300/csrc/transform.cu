@@ -727,7 +727,8 @@ cudaError_t launch_step_tables(const StepTableBuild& b, cudaStream_t st) {
 // ---------------------------------------------------------------------------------
 // Launchers: one instantiation per transform size. The lazy arithmetic covers
 // T <= 2^23 (one-CTA sizes 2^4..2^13, columns 2^6..2^11, rows 2^7..2^13); the wide
-// arithmetic covers T = 2^24, 2^25 (columns 2^12, rows 2^12..2^13).
+// arithmetic covers T = 2^24, 2^25 (columns 2^12, rows 2^12..2^13) and T = 2^22,
+// 2^23 when the wide primes save one (columns 2^10, rows 2^12..2^13).
 
 // Column residues plus the level root table (8-byte entries, 16-byte aligned); the
 // forward pass adds its per-sweep four-step factors (G rows of SW + 1 entries).
@@ -828,6 +829,7 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
 static cudaError_t fwd_cols_any(const TransformArgs& g, bool square, bool sign, cudaStream_t st, bool init) {
     if (g.wide) {
         if (g.log_r == 12) return fwd_cols_at<WideArith, 12>(g, square, sign, st, init);
+        if (g.log_r == 10) return fwd_cols_at<WideArith, 10>(g, square, sign, st, init);
         return cudaErrorInvalidValue;
     }
     switch (g.log_r) {
@@ -862,6 +864,7 @@ static cudaError_t rows_any(const TransformArgs& g, int mode, cudaStream_t st, b
 static cudaError_t inv_cols_any(const TransformArgs& g, cudaStream_t st, bool init) {
     if (g.wide) {
         if (g.log_r == 12) return inv_cols_at<WideArith, 12>(g, st, init);
+        if (g.log_r == 10) return inv_cols_at<WideArith, 10>(g, st, init);
         return cudaErrorInvalidValue;
     }
     switch (g.log_r) {
@@ -893,7 +896,7 @@ cudaError_t init_transform_kernels() {
                 for (int l = 6; l <= 13 && e == cudaSuccess; ++l) {
                     g.log_r = l;
                     g.log_c = l;
-                    const bool col_ok = w ? l == 12 : l <= 11;
+                    const bool col_ok = w ? l == 12 || l == 10 : l <= 11;
                     const bool row_ok = w ? l >= 12 : l >= 7;
                     if (col_ok) e = fwd_cols_any(g, sq, sg, 0, true);
                     for (int mode = 0; mode < 4 && e == cudaSuccess && row_ok && sg == 0 && sq == 0; ++mode)

@@ -436,14 +436,19 @@ def test_concurrent_host_calls_and_streams(gpu):
         w.close()
 
 
-def test_six_prime_products(ws, gpu):
-    # T = 2^22 and 2^23 with the shorter operand above 2^20 limbs need six primes
-    for la, lb in [(1 << 21, 1 << 21), (3 << 20, (1 << 21) + 3)]:
-        assert gpu.MulPlan.new(la, lb).primes == 6
+def test_wide_primes_at_2_pow_22_and_23(ws, gpu):
+    # T = 2^22 and 2^23 with the shorter operand above 2^20 (2^19) limbs: five lazy
+    # primes hold too few bits, five wide ones enough (canonical arithmetic on the
+    # 2^10-point column kernels); exact against the oracle
+    for la, lb in [(1 << 21, 1 << 21), (3 << 20, (1 << 21) + 3), (3_000_000, 1_500_000)]:
+        plan = gpu.MulPlan.new(la, lb)
+        assert plan.primes == 5 and plan.log_transform in (22, 23) and plan.blocks == 0, (la, lb)
         a, b = operand(la, 111), operand(lb, 112)
-        assert fingerprint_ok(a, b, gpu_mul(ws, a, b)), (la, lb)
+        assert np.array_equal(gpu_mul(ws, a, b), oracle.mul(a, b, THREADS)), (la, lb)
     ones = np.full(1 << 21, MASK, dtype=np.uint64)
     assert np.array_equal(gpu_mul(ws, ones, ones), all_ones_expected(1 << 21, 1 << 21))
+    a = operand(3 << 20, 113)
+    assert np.array_equal(gpu_sqr(ws, a), oracle.sqr(a, THREADS))
 
 
 def test_poisoned_scratch_and_any_shape_order(gpu):
