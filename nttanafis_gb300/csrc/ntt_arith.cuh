@@ -12,7 +12,9 @@
 //   Lazy  (p < 2^30): Harvey's lazy butterflies. Forward values lie in [0, 2p),
 //                     inverse values in [0, 4p); 4p < 2^32 keeps every sum in a u32.
 //   Wide  (p < 2^31): canonical values in [0, p). Used where no prime below 2^30
-//                     has the two-power roots of the transform (T >= 2^24).
+//                     has the two-power roots of the transform (T >= 2^24), and
+//                     at T = 2^22, 2^23 where five of them hold what six
+//                     lazy primes would.
 #pragma once
 #include <stdint.h>
 

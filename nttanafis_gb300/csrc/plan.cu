@@ -30,7 +30,8 @@ static const u32 kLazyPrimes[] = {
     595591169u,  576716801u,  469762049u, 463470593u, 459276289u, 415236097u, 387973121u,
     383778817u,  377487361u,
 };
-// Primes below 2^31 with valuation at least 24 (canonical arithmetic, T >= 2^24).
+// Primes below 2^31 with valuation at least 24 (canonical arithmetic): T >= 2^24,
+// and T = 2^22, 2^23 where they save a prime (choose_primes).
 static const u32 kWidePrimes[] = {
     2130706433u, 2113929217u, 2013265921u, 1811939329u, 1711276033u,
     1224736769u, 1107296257u, 754974721u,  469762049u,  167772161u,

@@ -254,22 +254,24 @@ def test_wide_block_split(ws):
 
 
 def test_wide_class_in_a_batch(gpu):
-    # a T = 2^24 member beside a short one: the 2^12-point column kernels in batch mode
+    # T = 2^24 and T = 2^22 wide members beside a short one: the 2^12- and 2^10-point
+    # column kernels of the wide arithmetic in batch mode
     import torch
 
     big_a, big_b = operand(1 << 23, 35), operand((1 << 23) - 7, 36)
+    mid_a, mid_b = operand(1 << 21, 39), operand((1 << 21) - 5, 40)
     small_a, small_b = operand(3000, 37), operand(2000, 38)
     batch = gpu.GpuBatch()
-    dev = [torch.from_numpy(x.view(np.int64)).cuda() for x in (big_a, big_b, small_a, small_b)]
-    d_big = torch.full((big_a.size + big_b.size + 1,), -1, dtype=torch.int64, device="cuda")
-    d_small = torch.full((small_a.size + small_b.size + 1,), -1, dtype=torch.int64, device="cuda")
-    reqs = [gpu.Request(d_big, dev[0], dev[1]), gpu.Request(d_small, dev[2], dev[3])]
+    dev = [torch.from_numpy(x.view(np.int64)).cuda() for x in (big_a, big_b, mid_a, mid_b, small_a, small_b)]
+    dsts = [torch.full((x.size + y.size + 1,), -1, dtype=torch.int64, device="cuda")
+            for x, y in ((big_a, big_b), (mid_a, mid_b), (small_a, small_b))]
+    reqs = [gpu.Request(dsts[i], dev[2 * i], dev[2 * i + 1]) for i in range(3)]
     assert batch.run(reqs, torch.cuda.current_stream()), gpu.last_error()
     torch.cuda.synchronize()
-    big = d_big.cpu().numpy().view(np.uint64)
-    small = d_small.cpu().numpy().view(np.uint64)
-    assert big[-1] == MASK and small[-1] == MASK
+    big, mid, small = (d.cpu().numpy().view(np.uint64) for d in dsts)
+    assert big[-1] == MASK and mid[-1] == MASK and small[-1] == MASK
     assert fingerprint_ok(big_a, big_b, big[:-1])
+    assert np.array_equal(mid[:-1], oracle.mul(mid_a, mid_b, THREADS))
     assert np.array_equal(small[:-1], oracle.mul(small_a, small_b, THREADS))
     assert batch.status() == 0
     batch.close()
