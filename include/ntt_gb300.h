@@ -307,8 +307,9 @@ uint8_t ntt_crt_pair_combine_device(uint64_t first, uint64_t second, int64_t* d_
  * (columns 2^6..2^11, rows 2^7..2^13). ntt_split_get returns the log_r in use (0
  * for lengths without a four-step split). The split changes speed, never results.
  * ntt_tune_splits times every split of each length in [min_log_t, max_log_t] on
- * balanced products that fill the transform (`reps` products per timing, best of
- * two) on `stream` and keeps the fastest when it beats the default by 2%; it
+ * products that fill the transform on the lazy primes (balanced up to 2^21 points,
+ * a 2^19-limb shorter operand above; `reps` products per timing, best of two) on
+ * `stream` and keeps the fastest when it beats the default by 2%; it
  * synchronizes `stream` and allocates its operands for the call. Calls made by other
  * threads meanwhile may run with a split under trial (their results stay exact). No
  * reference counterpart: the reference fixes its geometry in Geometry::select. */

@@ -508,30 +508,35 @@ uint8_t ntt_tune_splits(int min_log_t, int max_log_t, int reps, void* stream) {
     if (min_log_t > max_log_t) return 1;
     reps = std::max(1, reps);
     cudaStream_t st = (cudaStream_t)stream;
-    const u64 half = (u64)1 << (max_log_t - 1);
+    // The timed products fill the transform on the lazy primes, whose splits these
+    // are: balanced up to 2^21 points; above, a shorter operand of 2^19 limbs (a
+    // balanced product there takes the wide primes, whose split is fixed).
+    constexpr int kLazyShortLog = 19;
+    const u64 full = (u64)1 << max_log_t;
     u64 *a = nullptr, *b = nullptr, *dst = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ntt_mul_workspace* ws = ntt_mul_workspace_new();
-    bool ok = ws && cuda_ok(cudaMalloc(&a, half * 8), "cudaMalloc") && cuda_ok(cudaMalloc(&b, half * 8), "cudaMalloc") &&
-              cuda_ok(cudaMalloc(&dst, 2 * half * 8), "cudaMalloc") &&
+    bool ok = ws && cuda_ok(cudaMalloc(&a, full * 8), "cudaMalloc") && cuda_ok(cudaMalloc(&b, full / 2 * 8), "cudaMalloc") &&
+              cuda_ok(cudaMalloc(&dst, full * 8), "cudaMalloc") &&
               cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") && cuda_ok(cudaEventCreate(&e1), "cudaEventCreate") &&
-              cuda_ok(cudaMemsetAsync(a, 0xA5, half * 8, st), "cudaMemset") &&
-              cuda_ok(cudaMemsetAsync(b, 0x3C, half * 8, st), "cudaMemset");
+              cuda_ok(cudaMemsetAsync(a, 0xA5, full * 8, st), "cudaMemset") &&
+              cuda_ok(cudaMemsetAsync(b, 0x3C, full / 2 * 8, st), "cudaMemset");
     for (int log_t = min_log_t; ok && log_t <= max_log_t; ++log_t) {
         int lo = 0, hi = 0;
         if (!split_range(log_t, lo, hi) || lo == hi) continue;
-        // operands of 2^(log_t - 1) limbs: the product fills the transform
-        const u64 n = (u64)1 << (log_t - 1);
+        const u64 nb = (u64)1 << std::min(log_t - 1, log_t <= 21 ? log_t - 1 : kLazyShortLog);
+        const u64 na = ((u64)1 << log_t) - nb;  // na + nb - 1 coefficients fill 2^log_t points
         const int before = g_split[log_t].load();
         float best = 1e30f, standard = 1e30f;
         int pick = log_t / 2;
         for (int r = lo; ok && r <= hi; ++r) {
             g_split[log_t].store(r == log_t / 2 ? 0 : r);
-            ok = ntt_mul_workspace_mul_device(ws, dst, 2 * n, a, n, b, n, st) == 1;  // tables, warm-up
+            ok = ntt_mul_workspace_mul_device(ws, dst, na + nb, a, na, b, nb, st) == 1;  // tables, warm-up
             float ms = 1e30f;
             for (int round = 0; ok && round < 2; ++round) {
                 ok = cuda_ok(cudaEventRecord(e0, st), "cudaEventRecord");
-                for (int i = 0; ok && i < reps; ++i) ok = ntt_mul_workspace_mul_device(ws, dst, 2 * n, a, n, b, n, st) == 1;
+                for (int i = 0; ok && i < reps; ++i)
+                    ok = ntt_mul_workspace_mul_device(ws, dst, na + nb, a, na, b, nb, st) == 1;
                 float t = 0;
                 ok = ok && cuda_ok(cudaEventRecord(e1, st), "cudaEventRecord") &&
                      cuda_ok(cudaEventSynchronize(e1), "cudaEventSynchronize") &&
