@@ -22,6 +22,7 @@
 #include "transform_common.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace ntt {
 
@@ -334,6 +335,18 @@ constexpr int kCol4Vs = 65 * 64 + 32 / kCol4G;
 static_assert(kCol4Vs % 32 == 32 / kCol4G && step_log_u(kCol4LogR) == 6, "radix-64 column layout");
 static_assert(kCol4Threads * 128 * (kCol4LogG == 2 ? 2 : 1) <= 65536, "register budget of the column CTAs");
 
+// SMs of the current device (persistent kernels launch one CTA per SM).
+static int sm_count() {
+    static std::atomic<int> cached[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    int n = cached[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    cached[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
 static size_t col4_smem(bool fwd) {
     return (size_t)kCol4G * kCol4Vs * sizeof(u32) + 64 * sizeof(uint2) + (fwd ? kCol4G * 65 * sizeof(uint2) : 0);
 }
@@ -457,6 +470,98 @@ __global__ void __launch_bounds__(kCol4Threads, kCol4LogG == 2 ? 2 : 1)
 #pragma unroll
         for (int k = 0; k < E; ++k) q[(u64)(k * E) << log_c] = A::canonical(x[0][k], pp.p);
     }
+}
+
+// Persistent form of k_inv_cols4 (NTT_INV_COLS4_PERSIST): one CTA per SM loops
+// over the (column group, prime, member) items. Once an item's second pass holds
+// its points in registers, the shared buffer is free, and 16-byte cp.async copies
+// bring the next item's residues into it while that pass computes and stores, so
+// that the loads of one item overlap the butterflies of the one before. The copies
+// land in a raw layout, row 64b + k of the 8 columns at word 520b + 8k: the first
+// pass (rows 64 blk + k) reads it without bank conflicts, and it fits the buffer
+// (64 x 520 <= 8 x kCol4Vs words). The inverse roots of every prime sit after it.
+#ifndef NTT_INV_COLS4_PERSIST
+#define NTT_INV_COLS4_PERSIST 1
+#endif
+constexpr int kRawBlockWords = 520;
+static_assert(kCol4G == 8 && 64 * kRawBlockWords <= kCol4G * kCol4Vs && kRawBlockWords % 32 == 8,
+              "raw layout of the persistent inverse column pass");
+
+static size_t col4p_smem(int np) { return (size_t)kCol4G * kCol4Vs * sizeof(u32) + (size_t)np * 64 * sizeof(uint2); }
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <class A>
+__global__ void __launch_bounds__(kCol4Threads, 1) k_inv_cols4p(const __grid_constant__ TransformArgs g) {
+    extern __shared__ u32 sm[];
+    constexpr int G = kCol4G, LOG_G = kCol4LogG, VS = kCol4Vs, E = 64, RB = kRawBlockWords;
+    release_dependents();
+    const int log_c = g.log_c;
+    const u32 groups = 1u << (log_c - LOG_G), np = (u32)g.np;
+    const u32 items = groups * np * (u32)(g.batch ? g.count : 1);
+    const int c = threadIdx.x & (G - 1), blk = threadIdx.x >> LOG_G;
+    uint2* tw = reinterpret_cast<uint2*>(sm + G * VS);  // [prime][64] inverse roots
+    for (int i = threadIdx.x; i < g.np * 64; i += kCol4Threads) tw[i] = __ldg(g.ps.pr[i >> 6].inv + (i & 63));
+    wait_prior_grid();  // the row pass's output
+    // residues of item it: [prime][T] of its member, from column group * G
+    auto source = [&](u32 it) -> u32* {
+        const u32 group = it % groups, rest = it / groups;
+        const Member mm = member_of(g, (int)(rest / np), false);
+        return mm.spec + ((size_t)(rest % np) << g.log_t) + (size_t)group * G;
+    };
+    auto prefetch = [&](u32 it) {
+        const u32* src = source(it);
+        for (int j = threadIdx.x; j < 2 * 4096; j += kCol4Threads) {
+            const int r = j >> 1, h = j & 1;
+            cp_async16(sm + RB * (r >> 6) + 8 * (r & 63) + 4 * h, src + ((u64)r << log_c) + 4 * h);
+        }
+        cp_async_commit();
+    };
+    if (blockIdx.x < items) prefetch(blockIdx.x);
+    for (u32 it = blockIdx.x; it < items; it += gridDim.x) {
+        const u32 group = it % groups, rest = it / groups;
+        const int prime = (int)(rest % np), member = (int)(rest / np);
+        const PrimeParams& pp = g.ps.pr[prime];
+        // the CRT look-back flags of this product, cleared once every kernel before
+        // this one has completed
+        if (group == 0 && prime == 0) clear_flags(g, member);
+        cp_async_wait_all();
+        __syncthreads();
+        // Pass 1: levels 0-5 on rows 64 blk + k (bit-reversed spectrum in).
+        u32 x[1][E];
+        {
+            const u32* raw = sm + RB * blk + c;
+#pragma unroll
+            for (int k = 0; k < E; ++k) x[0][k] = raw[8 * k];
+            dit_levels<A, 6, 1, 1, 2>(x, tw + 64 * prime, pp.p);  // [0, 2p) in ([0, p) when wide)
+        }
+        __syncthreads();  // every raw read is done before the padded layout overwrites it
+        {
+            u32* base = sm + c * VS + 65 * blk;
+#pragma unroll
+            for (int k = 0; k < E; ++k) base[k] = x[0][k];
+        }
+        __syncthreads();
+        // Pass 2: levels 6-11 on rows blk + 64k, canonical residues out; the next
+        // item's residues come in behind it.
+        {
+            const u32* base = sm + c * VS + blk;
+#pragma unroll
+            for (int k = 0; k < E; ++k) x[0][k] = base[65 * k];
+        }
+        __syncthreads();
+        if (it + gridDim.x < items) prefetch(it + gridDim.x);
+        dit_levels<A, 6, E, 1>(x, pp.inv + blk, pp.p);
+        u32* q = source(it) + c + ((u64)blk << log_c);
+#pragma unroll
+        for (int k = 0; k < E; ++k) q[(u64)(k * E) << log_c] = A::canonical(x[0][k], pp.p);
+    }
+    cp_async_wait_all();
 }
 
 // Rows per CTA of the row pass: enough that every thread owns a register block of
@@ -816,6 +921,13 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
         return launch_dependent(k, grid, dim3(kThreads), col2_smem(false), st, g);
     } else if constexpr (L == kCol4LogR) {
+        if (NTT_INV_COLS4_PERSIST) {
+            auto k = k_inv_cols4p<A>;
+            if (init) return opt_in(k, NTT_COLS_CARVEOUT);
+            const unsigned items = grid.x * grid.y * grid.z;
+            return launch_dependent(k, dim3(std::min(items, (unsigned)sm_count())), dim3(kCol4Threads),
+                                    col4p_smem(g.np), st, g);
+        }
         auto k = k_inv_cols4<A>;
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
         return launch_dependent(k, grid, dim3(kCol4Threads), col4_smem(false), st, g);
