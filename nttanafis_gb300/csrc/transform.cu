@@ -921,7 +921,7 @@ static cudaError_t inv_cols_at(const TransformArgs& g, cudaStream_t st, bool ini
         if (init) return opt_in(k, NTT_COLS_CARVEOUT);
         return launch_dependent(k, grid, dim3(kThreads), col2_smem(false), st, g);
     } else if constexpr (L == kCol4LogR) {
-        if (NTT_INV_COLS4_PERSIST) {
+        if constexpr (NTT_INV_COLS4_PERSIST) {
             auto k = k_inv_cols4p<A>;
             if (init) return opt_in(k, NTT_COLS_CARVEOUT);
             const unsigned items = grid.x * grid.y * grid.z;
