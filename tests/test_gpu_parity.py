@@ -438,6 +438,21 @@ def test_concurrent_host_calls_and_streams(gpu):
         w.close()
 
 
+@pytest.mark.parametrize("log_t,lb", [(23, 1 << 19), (23, (1 << 19) + 1), (23, (1 << 20) + 1), (22, 1 << 20),
+                                      (22, (1 << 20) + 1)])
+def test_all_ones_at_the_lazy_wide_boundary(ws, gpu, log_t, lb):
+    # 2^log_t points filled: a shorter operand of 2^19 limbs at 2^23 (2^20 at 2^22)
+    # needs exactly the capacity of five lazy primes there (147, 148 bits); one limb
+    # more takes five wide primes. All-ones operands give the largest coefficients
+    # (closed form, src/tests/scheduling.rs:35-45).
+    la = (1 << log_t) - lb
+    plan = gpu.MulPlan.new(la, lb)
+    assert plan.primes == 5 and plan.log_transform == log_t and plan.blocks == 0
+    a = np.full(la, MASK, dtype=np.uint64)
+    b = np.full(lb, MASK, dtype=np.uint64)
+    assert np.array_equal(gpu_mul(ws, a, b), all_ones_expected(la, lb))
+
+
 def test_wide_primes_at_2_pow_22_and_23(ws, gpu):
     # T = 2^22 and 2^23 with the shorter operand above 2^20 (2^19) limbs: five lazy
     # primes hold too few bits, five wide ones enough (canonical arithmetic on the
