@@ -66,3 +66,31 @@ def test_unbalanced_4m_by_1024(gpu, cws, bits, signed):
     assert np.array_equal(got, oracle.conv(a, b, mx, mx, signed, THREADS)), (bits, signed)
     _, swapped = convolve(gpu, cws, b, a, mx, signed)
     assert np.array_equal(swapped, got)
+
+
+def test_wide_prime_convolution_at_2_pow_22(gpu, cws):
+    # 64-bit unsigned coefficients, the shorter operand above 2^20 terms: the bound
+    # needs 149 bits, five wide primes (five lazy ones hold 148 at 2^22); maximal
+    # coefficients, exact against the oracle, and admission on the wide column pass
+    import torch
+
+    mx = (1 << 64) - 1
+    la, lb = 3 * (1 << 20) - 7, (1 << 20) + 3
+    a = np.full(la, MASK, dtype=np.uint64)
+    b = operand(lb, 501)
+    b[::3] = np.uint64(MASK)
+    plan, got = convolve(gpu, cws, a, b, mx, False)
+    assert plan.log_transform == 22 and plan.primes == 5 and plan.stride() == 3
+    assert np.array_equal(got, oracle.conv(a, b, mx, mx, False, THREADS))
+    # a bound one below the maximum rejects the all-ones operand on the device path
+    stream = torch.cuda.current_stream()
+    small = gpu.ConvPlan.new(la, lb, mx - 1, mx - 1, False)
+    w = gpu.GpuConvWorkspace()
+    assert w.prepare(small)
+    dst = torch.full((small.output_len(),), -1, dtype=torch.int64, device="cuda")
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    db = torch.from_numpy((b & np.uint64(mx - 1)).view(np.int64)).cuda()
+    assert w.convolve_device(dst, da, db, stream)
+    torch.cuda.synchronize()
+    assert w.status() == gpu.STATUS_BOUND and bool((dst == -1).all())
+    w.close()
