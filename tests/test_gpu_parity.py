@@ -245,12 +245,16 @@ def test_wide_prime_class_2_pow_24(ws):
     assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
 
 
-def test_wide_block_split(ws):
+def test_wide_block_split(ws, gpu):
     # blocks of 2^24-point transforms (wide primes) sharing the shorter operand's
-    # spectrum: the 2^12-point column kernels in their one-operand spectrum mode
-    a, b = operand(40_000_000, 33), operand(2_000_000, 34)
-    assert fingerprint_ok(a, b, gpu_mul(ws, a, b))
-    assert fingerprint_ok(a, b, gpu_mul(ws, b, a))
+    # spectrum: the 2^12-point column kernels in their one-operand spectrum mode;
+    # blocks of 2^23 and 2^22 points on the wide primes: the 2^10-point ones
+    for la, lb, log_t in [(40_000_000, 2_000_000, 24), (20_000_000, 1_500_000, 23), (12_000_000, 1_100_000, 22)]:
+        plan = gpu.MulPlan.new(la, lb)
+        assert plan.blocks > 1 and plan.log_transform == log_t and plan.primes == 5, (la, lb)
+        a, b = operand(la, 33), operand(lb, 34)
+        assert fingerprint_ok(a, b, gpu_mul(ws, a, b)), (la, lb)
+        assert fingerprint_ok(a, b, gpu_mul(ws, b, a)), (la, lb)
 
 
 def test_wide_class_in_a_batch(gpu):
