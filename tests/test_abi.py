@@ -109,6 +109,23 @@ def test_plans_hold_every_coefficient():
             assert (1 << p.log_transform) >= la + lb - 1
 
 
+def test_fewest_primes_per_length():
+    # five primes hold every product: lazy ones up to 2^21 points and where they
+    # suffice at 2^22 (148 bits) and 2^23 (147); wide ones beyond, and at 2^22, 2^23
+    # where five lazy primes fall a bit short (six would be needed)
+    for la, lb in [(1024, 1024), (2**20, 2**20), ((1 << 22) - 2**20, 2**20), ((1 << 22) - 2**20 - 1, 2**20 + 1),
+                   ((1 << 23) - 2**19, 2**19), ((1 << 23) - 2**19 - 1, 2**19 + 1), (2**22, 2**22), (2**24, 2**24)]:
+        p = ntt.MulPlan.new(la, lb)
+        assert p.primes == 5 and p.blocks == 0, (la, lb)
+        assert p.log_transform == max(4, (la + lb - 2).bit_length()), (la, lb)
+    # convolutions: 16-bit and 32-bit classes unchanged, 64-bit coefficients over
+    # 2^20 terms at 2^22 points on five primes (149 bits)
+    assert ntt.ConvPlan.new(2**22, 2**22, 0xFFFF, 0xFFFF, False).primes == 2
+    assert ntt.ConvPlan.new(2**22, 2**22, 2**32 - 1, 2**32 - 1, False).primes == 3
+    wide = ntt.ConvPlan.new(3 * 2**20 - 7, 2**20 + 3, 2**64 - 1, 2**64 - 1, False)
+    assert wide.primes == 5 and wide.log_transform == 22 and wide.stride() == 3
+
+
 def test_block_split_choice():
     # very unbalanced shapes split; balanced ones and squares never do
     assert ntt.MulPlan.new(2**20, 1024).blocks > 1
